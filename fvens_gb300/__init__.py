@@ -1,0 +1,263 @@
+"""Python binding of the fvens_gb300 C ABI (include/fvens_gb300.h).
+
+A thin ctypes layer over the CUDA library built by ``fvens_gb300.build``.
+Class and method names mirror the reference's host interfaces
+(UMesh, FlowFV::compute_residual / assemble_jacobian / getGradients,
+SteadyBackwardEulerSolver::solve) so call sites keep their shape.
+Device arrays are passed as CUDA tensors (torch) or raw integer addresses;
+there is no CPU path: if the CUDA library is missing, loading fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libfvens_gb300.so")
+
+FV_OK, FV_ERR_INVALID, FV_ERR_CUDA, FV_ERR_NUMERICAL, FV_ERR_TOLERANCE, FV_ERR_UNSUPPORTED, FV_ERR_MESH = range(7)
+FLUX = {"LLF": 0, "VANLEER": 1, "AUSM": 2, "AUSMPLUS": 3, "ROE": 4, "HLL": 5, "HLLC": 6}
+GRADIENT = {"NONE": 0, "GREENGAUSS": 1, "LEASTSQUARES": 2}
+RECONSTRUCTION = {"NONE": 0, "VANALBADA": 1, "BARTHJESPERSEN": 2, "VENKATAKRISHNAN": 3, "WENO": 4}
+BC = {"slipwall": 0, "farfield": 1, "inflowoutflow": 2, "subsonic_inflow": 3, "extrapolation": 4,
+      "periodic": 5, "isothermalwall": 6, "adiabaticwall": 7}
+PC = {"none": 0, "jacobi": 1, "sgs": 2, "ilu0": 3}
+MESH_CHANNEL_BUMP, MESH_NACA_OGRID = 1, 2
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+
+class FvensError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"fvens_gb300 status {status}: {message}")
+        self.status = status
+
+
+class fv_mesh_desc(ctypes.Structure):
+    _fields_ = [("npoin", ctypes.c_int), ("nelem", ctypes.c_int), ("nbface", ctypes.c_int),
+                ("coords", _c_dbl_p), ("nnode", _c_int_p), ("inpoel", _c_int_p),
+                ("bface", _c_int_p), ("btag", _c_int_p)]
+
+
+class fv_physics_cfg(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("Minf", ctypes.c_double), ("Tinf", ctypes.c_double),
+                ("Reinf", ctypes.c_double), ("Pr", ctypes.c_double), ("aoa", ctypes.c_double),
+                ("viscous_sim", ctypes.c_int), ("const_visc", ctypes.c_int)]
+
+
+class fv_numerics_cfg(ctypes.Structure):
+    _fields_ = [("conv_numflux", ctypes.c_int), ("conv_numflux_jac", ctypes.c_int),
+                ("gradientscheme", ctypes.c_int), ("reconstruction", ctypes.c_int),
+                ("limiter_param", ctypes.c_double), ("order2", ctypes.c_int)]
+
+
+class fv_bc_cfg(ctypes.Structure):
+    _fields_ = [("bc_tag", ctypes.c_int), ("bc_type", ctypes.c_int), ("bc_vals", ctypes.c_double * 2)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"fvens_gb300 CUDA library not found at {LIB_PATH}; "
+                               "run `python -m fvens_gb300.build` (no CPU fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        L.fv_status_string.restype = ctypes.c_char_p
+        L.fv_last_error.restype = ctypes.c_char_p
+        L.fv_kernel_launch_count.restype = ctypes.c_longlong
+        L.fv_mesh_destroy.restype = None
+        L.fv_disc_destroy.restype = None
+        L.fv_matrix_destroy.restype = None
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != FV_OK:
+        L = lib()
+        raise FvensError(status, L.fv_last_error().decode() or L.fv_status_string(status).decode())
+
+
+def dptr(x):
+    """Device address of a CUDA tensor (or a raw integer address)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return x.data_ptr()
+    raise TypeError(f"cannot take a device address of {type(x)}")
+
+
+def _hp(a, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+class UMesh:
+    """Unstructured 2-D mesh (reference UMesh + preprocessMesh)."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle) if isinstance(handle, int) else handle
+        c = (ctypes.c_int * 6)()
+        check(lib().fv_mesh_counts(self._h, c))
+        self.nelem, self.nbface, self.ninface, self.naface, self.npoin, self.ncolors = list(c)
+
+    @classmethod
+    def from_arrays(cls, coords, nnode, inpoel, bface, btag, reorder=0):
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        nnode = np.ascontiguousarray(nnode, dtype=np.int32)
+        inpoel = np.ascontiguousarray(inpoel, dtype=np.int32)
+        bface = np.ascontiguousarray(bface, dtype=np.int32)
+        btag = np.ascontiguousarray(btag, dtype=np.int32)
+        d = fv_mesh_desc(coords.shape[0], nnode.shape[0], btag.shape[0], _hp(coords, ctypes.c_double),
+                         _hp(nnode, ctypes.c_int), _hp(inpoel, ctypes.c_int), _hp(bface, ctypes.c_int),
+                         _hp(btag, ctypes.c_int))
+        h = ctypes.c_void_p()
+        check(lib().fv_mesh_create(ctypes.byref(d), int(reorder), ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def generate(cls, kind, params, reorder=1):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        h = ctypes.c_void_p()
+        check(lib().fv_mesh_generate(int(kind), _hp(p, ctypes.c_double), len(p), int(reorder), ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_gmsh(cls, path, reorder=0):
+        h = ctypes.c_void_p()
+        check(lib().fv_mesh_read_gmsh(path.encode(), int(reorder), ctypes.byref(h)))
+        return cls(h)
+
+    def export(self):
+        coords = np.zeros((self.npoin, 2))
+        nnode = np.zeros(self.nelem, np.int32)
+        inpoel = np.zeros((self.nelem, 4), np.int32)
+        bface = np.zeros((self.nbface, 2), np.int32)
+        btag = np.zeros(self.nbface, np.int32)
+        perm = np.zeros(self.nelem, np.int32)
+        check(lib().fv_mesh_export(self._h, _hp(coords, ctypes.c_double), _hp(nnode, ctypes.c_int),
+                                   _hp(inpoel, ctypes.c_int), _hp(bface, ctypes.c_int), _hp(btag, ctypes.c_int),
+                                   _hp(perm, ctypes.c_int)))
+        return dict(coords=coords, nnode=nnode, inpoel=inpoel, bface=bface, btag=btag, perm=perm)
+
+    def geometry(self):
+        face_lr = np.zeros((self.naface, 2), np.int32)
+        fnorm = np.zeros((self.naface, 3))
+        area = np.zeros(self.nelem)
+        cc = np.zeros((self.nelem, 2))
+        color = np.zeros(self.nelem, np.int32)
+        check(lib().fv_mesh_geometry(self._h, _hp(face_lr, ctypes.c_int), _hp(fnorm, ctypes.c_double),
+                                     _hp(area, ctypes.c_double), _hp(cc, ctypes.c_double), _hp(color, ctypes.c_int)))
+        return dict(face_lr=face_lr, fnorm=fnorm, area=area, cc=cc, color=color)
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fv_mesh_destroy(self._h)
+            self._h = None
+
+
+def physics_cfg(gamma=1.4, Minf=0.5, Tinf=288.15, Reinf=float("inf"), Pr=0.72, aoa_deg=0.0, viscous=False,
+                const_visc=False):
+    return fv_physics_cfg(gamma, Minf, Tinf, Reinf, Pr, np.deg2rad(aoa_deg), int(viscous), int(const_visc))
+
+
+def numerics_cfg(flux="ROE", flux_jac=None, gradient="LEASTSQUARES", reconstruction="NONE", limiter_param=0.0,
+                 order2=None):
+    flux_jac = flux if flux_jac in (None, "CONSISTENT") else flux_jac
+    if order2 is None:
+        order2 = gradient != "NONE"
+    return fv_numerics_cfg(FLUX[flux], FLUX[flux_jac], GRADIENT[gradient], RECONSTRUCTION[reconstruction],
+                           float(limiter_param), int(order2))
+
+
+class FlowFV:
+    """GPU finite-volume flow discretisation of `batch` conditions on one mesh
+    (reference FlowFV<scalar, order2, constVisc>)."""
+
+    def __init__(self, mesh, phys, numerics, bcs):
+        self.mesh = mesh
+        phys = list(phys) if isinstance(phys, (list, tuple)) else [phys]
+        self.batch = len(phys)
+        self._phys = (fv_physics_cfg * self.batch)(*phys)
+        self._num = numerics
+        bl = [fv_bc_cfg(int(t), BC[k] if isinstance(k, str) else int(k), (ctypes.c_double * 2)(*(list(v) + [0, 0])[:2]))
+              for (t, k, v) in bcs]
+        self._bcs = (fv_bc_cfg * max(len(bl), 1))(*bl)
+        h = ctypes.c_void_p()
+        check(lib().fv_disc_create(mesh._h, self._phys, self.batch, ctypes.byref(self._num), self._bcs, len(bl),
+                                   ctypes.byref(h)))
+        self._h = h
+        self.nelem = mesh.nelem
+
+    def set_stream(self, stream):
+        check(lib().fv_disc_set_stream(self._h, _vp(stream)))
+
+    def synchronize(self):
+        check(lib().fv_disc_synchronize(self._h))
+
+    def freestream(self):
+        u = np.zeros((self.batch, 4))
+        check(lib().fv_disc_freestream(self._h, _hp(u, ctypes.c_double)))
+        return u
+
+    def compute_residual(self, u, r, gettimesteps=False, dt=None):
+        """r += -R(u) (device arrays); dt receives local time steps when requested."""
+        check(lib().fv_compute_residual(self._h, _vp(dptr(u)), _vp(dptr(r)), int(bool(gettimesteps)),
+                                        _vp(dptr(dt)) if dt is not None else None))
+
+    def get_gradients(self, u, grad, primitive=False):
+        check(lib().fv_get_gradients(self._h, _vp(dptr(u)), _vp(dptr(grad)), int(bool(primitive))))
+
+    def assemble_jacobian(self, u, matrix):
+        check(lib().fv_assemble_jacobian(self._h, _vp(dptr(u)), matrix._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fv_disc_destroy(self._h)
+            self._h = None
+
+
+class BlockMatrix:
+    """Jacobian storage (PETSc BAIJ(4) equivalent), FP32 (precision 4) or FP64 (8)."""
+
+    def __init__(self, disc, precision=4):
+        self.disc = disc
+        h = ctypes.c_void_p()
+        check(lib().fv_matrix_create(disc._h, int(precision), ctypes.byref(h)))
+        self._h = h
+        self.precision = precision
+
+    def add_diagonal(self, diag):
+        check(lib().fv_matrix_add_diagonal(self.disc._h, self._h, _vp(dptr(diag))))
+
+    def to_host(self, member=0):
+        nnzb = ctypes.c_int()
+        L = lib()
+        check(L.fv_matrix_to_host(self.disc._h, self._h, int(member), ctypes.byref(nnzb), None, None, None))
+        n = self.disc.nelem
+        rowptr = np.zeros(n + 1, np.int32)
+        col = np.zeros(nnzb.value, np.int32)
+        val = np.zeros((nnzb.value, 16))
+        check(L.fv_matrix_to_host(self.disc._h, self._h, int(member), ctypes.byref(nnzb), _hp(rowptr, ctypes.c_int),
+                                  _hp(col, ctypes.c_int), _hp(val, ctypes.c_double)))
+        return rowptr, col, val
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fv_matrix_destroy(self._h)
+            self._h = None
+
+
+def kernel_launch_count():
+    return int(lib().fv_kernel_launch_count())

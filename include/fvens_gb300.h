@@ -1,0 +1,180 @@
+/*
+ * fvens_gb300 — C ABI of the GB300 (sm_103a) steady implicit flow hot path.
+ *
+ * The entry points replace the reference's spatial-discretisation and
+ * steady-solver interfaces (paths relative to the reference project):
+ *   Spatial / FlowFV            src/spatial/aspatial.hpp:37-167,
+ *                               src/spatial/flow_spatial.hpp:61-324
+ *   FlowPhysicsConfig,
+ *   FlowNumericsConfig          src/spatial/flow_spatial.hpp:33-55
+ *   FlowBCConfig                src/spatial/abc.hpp:34-40
+ *   UMesh construction          src/mesh/mesh.hpp, src/mesh/ameshutils.cpp:102-157
+ *   SteadyBackwardEulerSolver   src/ode/aodesolver.hpp, aodesolver.cpp:363-638
+ *   KSP/PC (PETSc, external)    FGMRES + bjacobi/ILU(0), SOR, point-block Jacobi
+ *
+ * Conventions
+ *   - Plain C types only.  Device pointers (d_*) point to CUDA global memory;
+ *     host pointers (h_*) to host memory.
+ *   - State vectors are the reference's PETSc block layout: nelem x 4 doubles
+ *     per flow condition (rho, rho*u, rho*v, rho*E), row-major; a batch of B
+ *     conditions on one mesh is B such vectors back to back.
+ *   - Calls on a handle are ordered on that handle's CUDA stream
+ *     (fv_disc_set_stream); device-pointer calls return before the GPU work
+ *     completes unless stated otherwise.  Host-pointer calls synchronise.
+ *   - No exception crosses the ABI: every call returns an fv_status; the
+ *     reference's Numerical_error / Tolerance_error map to FV_ERR_NUMERICAL /
+ *     FV_ERR_TOLERANCE.  fv_last_error() describes the most recent failure of
+ *     the calling thread.
+ *   - Handles are not reentrant: one thread at a time per handle, as the
+ *     reference's FlowFV::compute_residual (flow_spatial.hpp:190-198).
+ */
+#ifndef FVENS_GB300_H
+#define FVENS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int fv_status;
+#define FV_OK 0
+#define FV_ERR_INVALID 1      /* bad argument or configuration */
+#define FV_ERR_CUDA 2         /* CUDA runtime failure (no device, launch or memory error) */
+#define FV_ERR_NUMERICAL 3    /* non-finite residual norm (reference: Numerical_error) */
+#define FV_ERR_TOLERANCE 4    /* max steps reached (reference: Tolerance_error) */
+#define FV_ERR_UNSUPPORTED 5  /* option the reference does not implement (e.g. VanLeer Jacobian) */
+#define FV_ERR_MESH 6         /* mesh topology/geometry error */
+
+/* inviscid fluxes (afactory.cpp:31-92 names) */
+#define FV_FLUX_LLF 0
+#define FV_FLUX_VANLEER 1
+#define FV_FLUX_AUSM 2
+#define FV_FLUX_AUSMPLUS 3
+#define FV_FLUX_ROE 4
+#define FV_FLUX_HLL 5
+#define FV_FLUX_HLLC 6
+/* gradients (afactory.cpp:103-139) */
+#define FV_GRAD_NONE 0
+#define FV_GRAD_GREENGAUSS 1
+#define FV_GRAD_LEASTSQUARES 2
+/* reconstructions / limiters (afactory.cpp:168-227) */
+#define FV_REC_NONE 0
+#define FV_REC_VANALBADA 1
+#define FV_REC_BARTHJESPERSEN 2
+#define FV_REC_VENKATAKRISHNAN 3
+#define FV_REC_WENO 4
+/* boundary conditions: the reference's BCType numbering (abctypes.hpp) */
+#define FV_BC_SLIPWALL 0
+#define FV_BC_FARFIELD 1
+#define FV_BC_INFLOW_OUTFLOW 2
+#define FV_BC_SUBSONIC_INFLOW 3
+#define FV_BC_EXTRAPOLATION 4
+#define FV_BC_PERIODIC 5
+#define FV_BC_ISOTHERMALWALL 6
+#define FV_BC_ADIABATICWALL 7
+/* preconditioners (PETSc -pc_type pbjacobi / sor / bjacobi+ilu) */
+#define FV_PC_NONE 0
+#define FV_PC_JACOBI 1
+#define FV_PC_SGS 2
+#define FV_PC_ILU0 3
+/* synthetic meshes for fv_mesh_generate */
+#define FV_MESH_CHANNEL_BUMP 1  /* params: nx, ny, split_fraction, seed */
+#define FV_MESH_NACA_OGRID 2    /* params: nc, nr, rfar, nbl, h0, growth, tri_from_ring, seed */
+
+typedef struct fv_mesh fv_mesh;
+typedef struct fv_disc fv_disc;
+typedef struct fv_matrix fv_matrix;
+
+/* ---- utilities ---- */
+const char *fv_status_string(fv_status s);
+const char *fv_last_error(void);
+/* Number of CUDA kernels this library has launched in the process so far. */
+long long fv_kernel_launch_count(void);
+
+/* ---- mesh: UMesh + preprocessMesh (mesh.cpp, ameshutils.cpp:39-157) ---- */
+typedef struct {
+	int npoin, nelem, nbface;
+	const double *coords; /* npoin x 2 */
+	const int *nnode;     /* nelem, 3 or 4 */
+	const int *inpoel;    /* nelem x 4, counter-clockwise, -1 padded */
+	const int *bface;     /* nbface x 2 node indices */
+	const int *btag;      /* nbface boundary markers */
+} fv_mesh_desc;
+
+/* reorder: 0 keep the input cell order, 1 reverse Cuthill-McKee (-mesh_reorder rcm). */
+fv_status fv_mesh_create(const fv_mesh_desc *desc, int reorder, fv_mesh **out);
+fv_status fv_mesh_generate(int kind, const double *params, int nparams, int reorder, fv_mesh **out);
+/* Gmsh 2.2 ASCII (meshreaders.cpp:66-265) */
+fv_status fv_mesh_read_gmsh(const char *path, int reorder, fv_mesh **out);
+/* counts: nelem, nbface, ninface, naface, npoin, ncolors */
+fv_status fv_mesh_counts(const fv_mesh *m, int counts[6]);
+/* The mesh as built (cells in their final order, boundary faces oriented);
+ * perm[k] = input index of cell k.  Any pointer may be NULL. */
+fv_status fv_mesh_export(const fv_mesh *m, double *coords, int *nnode, int *inpoel, int *bface, int *btag, int *perm);
+/* face_lr: naface x 2 (left, right; right = -1-ib on boundary face ib);
+ * fnorm: naface x 3 (nx, ny, len); area: nelem; cc: nelem x 2; color: nelem */
+fv_status fv_mesh_geometry(const fv_mesh *m, int *face_lr, double *fnorm, double *area, double *cc, int *color);
+void fv_mesh_destroy(fv_mesh *m);
+
+/* ---- spatial discretisation: FlowFV<freal,order2,constVisc> (afactory.cpp:252-276) ---- */
+typedef struct {
+	double gamma, Minf, Tinf, Reinf, Pr;
+	double aoa;          /* radians */
+	int viscous_sim, const_visc;
+} fv_physics_cfg;
+typedef struct {
+	int conv_numflux, conv_numflux_jac, gradientscheme, reconstruction;
+	double limiter_param;
+	int order2;
+} fv_numerics_cfg;
+typedef struct {
+	int bc_tag, bc_type;
+	double bc_vals[2];
+} fv_bc_cfg;
+
+/* One discretisation of `batch` flow conditions on one mesh (phys[batch]). */
+fv_status fv_disc_create(fv_mesh *m, const fv_physics_cfg *phys, int batch, const fv_numerics_cfg *num,
+                         const fv_bc_cfg *bcs, int nbc, fv_disc **out);
+void fv_disc_destroy(fv_disc *d);
+/* cudaStream_t passed as void*; NULL = legacy default stream */
+fv_status fv_disc_set_stream(fv_disc *d, void *stream);
+fv_status fv_disc_synchronize(fv_disc *d);
+/* freestream conserved states (IdealGasPhysics::compute_freestream_state), batch x 4 */
+fv_status fv_disc_freestream(const fv_disc *d, double *h_uinf);
+
+/* Spatial::compute_residual (aspatial.hpp:64): d_r += -R(d_u); when
+ * gettimesteps, d_dt[nelem*batch] receives the local time steps. */
+fv_status fv_compute_residual(fv_disc *d, const double *d_u, double *d_r, int gettimesteps, double *d_dt);
+/* FlowFV_base::getGradients (flow_spatial.cpp:95-112): conserved-variable
+ * cell gradients, nelem x 8 per condition in GradBlock_t order
+ * ((x,v0),(y,v0),(x,v1),...).  With primitive != 0: the primitive-variable
+ * gradients the second-order residual uses. */
+fv_status fv_get_gradients(fv_disc *d, const double *d_u, double *d_grad, int primitive);
+
+/* ---- Jacobian: Spatial::assemble_jacobian (aspatial.cpp:242-340) ---- */
+/* precision 4: FP32 blocks, 8: FP64 blocks */
+fv_status fv_matrix_create(fv_disc *d, int precision, fv_matrix **out);
+void fv_matrix_destroy(fv_matrix *A);
+fv_status fv_assemble_jacobian(fv_disc *d, const double *d_u, fv_matrix *A);
+/* Adds d_diag[cell] * I to the diagonal blocks (addPseudoTimeTerm, aodesolver.cpp:300-329). */
+fv_status fv_matrix_add_diagonal(fv_disc *d, fv_matrix *A, const double *d_diag);
+/* Block-CSR copy of condition `member` (columns sorted, diagonal included):
+ * rowptr[nelem+1], col[nnzb], val[nnzb*16] (row-major 4x4).  Pass val == NULL
+ * to get nnzb only.  Synchronises. */
+fv_status fv_matrix_to_host(fv_disc *d, const fv_matrix *A, int member, int *nnzb, int *rowptr, int *col,
+                            double *val);
+
+/* ---- pointwise device evaluations (for validation against the reference) ---- */
+/* n states: d_ul, d_ur n x 4, d_n n x 2 -> d_f n x 4 (condition 0's physics) */
+fv_status fv_pointwise_flux(fv_disc *d, int kind, int n, const double *d_ul, const double *d_ur, const double *d_nrm,
+                            double *d_f);
+/* flux Jacobian blocks in the reference's convention: d_dfdl = -dF/dul, d_dfdr = dF/dur (n x 16) */
+fv_status fv_pointwise_flux_jacobian(fv_disc *d, int kind, int n, const double *d_ul, const double *d_ur,
+                                     const double *d_nrm, double *d_dfdl, double *d_dfdr);
+/* ghost states and BC Jacobians for BC kind bc_type with values bc_vals */
+fv_status fv_pointwise_bc(fv_disc *d, int bc_type, const double *bc_vals, int n, const double *d_in,
+                          const double *d_nrm, double *d_ghost, double *d_jac_ghost, double *d_dgdu);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1315,6 +1315,23 @@ int orc_residual_internals(const void *h, const double *u, double *grad, double 
 	if (uright) std::memcpy(uright, w.uright.data(), sizeof(double) * w.uright.size());
 	return 0;
 }
+/* per cell: sum over its faces of |F_k * len| (max over k), the scale the
+ * residual parity metric is normalised by */
+int orc_flux_scale(const void *h, const double *u, double *scale)
+{
+	const Disc *d = (const Disc *)h;
+	Disc::Work w;
+	std::vector<double> r(4 * (size_t)d->nelem(), 0.0);
+	d->residual(u, r.data(), false, nullptr, w);
+	const Mesh &M = *d->m;
+	for (int i = 0; i < M.nelem; i++) {
+		double s[4] = {0, 0, 0, 0};
+		for (int k = M.cf_ptr[i]; k < M.cf_ptr[i + 1]; k++)
+			for (int v = 0; v < 4; v++) s[v] += std::fabs(w.fflux[4 * M.cf_face[k] + v]);
+		scale[i] = std::max(std::max(s[0], s[1]), std::max(s[2], s[3]));
+	}
+	return 0;
+}
 int orc_conserved_gradients(const void *h, const double *u, double *grad)
 {
 	((const Disc *)h)->conserved_gradients(u, grad);

@@ -12,7 +12,7 @@ if [ ! -d "$REF/src" ]; then
   exit 0
 fi
 mkdir -p "$OUT"
-g++ -std=c++14 -O2 -fPIC -shared -w \
+g++ -std=c++14 -O2 -ffp-contract=off -fPIC -shared -w \
     -I"$HERE/eigen_stub" -I"$REF/src" \
     "$HERE/ref_wrap.cpp" -o "$OUT/libfvens_ref.so"
 echo "built $OUT/libfvens_ref.so"
