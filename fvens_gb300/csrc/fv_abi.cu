@@ -13,15 +13,10 @@
 #include "../../include/fvens_gb300.h"
 #include "fv_core.cuh"
 #include "fv_abi_internal.hpp"
+#include "fv_setup.hpp"
 
 using namespace fvg;
 
-struct fv_mesh : fv_mesh_impl {};
-struct fv_disc : fv_disc_impl {};
-struct fv_matrix {
-	BlockMatrix A;
-	fv_disc *owner = nullptr;
-};
 
 namespace fvg {
 
@@ -63,37 +58,13 @@ static fv_status mesh_upload(fv_mesh_impl *m)
 	if (m->dev_ready) return FV_OK;
 	const HostMesh &h = m->h;
 	DevMesh &d = m->d;
-	const int ne = h.nelem, nf = h.naface, nb = h.nbface;
-	d.nelem = ne; d.nbface = nb; d.naface = nf; d.ncolors = h.ncolors;
-	std::vector<double2> cc(ne), fcen(nf), gcen(std::max(nb, 1));
-	std::vector<double> area(ne), iarea(ne);
-	std::vector<int4> cface(ne), cnbr(ne), crev(ne);
-	std::vector<int2> flr(nf), fslot(nf);
-	std::vector<d4> fgeo(nf);
-	for (int i = 0; i < ne; i++) {
-		cc[i] = make_double2(h.cc[2 * i], h.cc[2 * i + 1]);
-		area[i] = h.area[i];
-		iarea[i] = 1.0 / h.area[i];
-		int cf[4], cn[4], rv[4];
-		for (int j = 0; j < 4; j++) {
-			if (j >= h.nnode[i]) { cf[j] = -1; cn[j] = -2; rv[j] = -1; continue; }
-			const int f = h.elemface[4 * i + j];
-			const int side = h.face_l[f] == i ? 0 : 1;
-			cf[j] = (f << 1) | side;
-			cn[j] = h.esuel[4 * i + j];
-			rv[j] = cn[j] >= 0 ? (side ? h.face_sl[f] : h.face_sr[f]) : -1;
-		}
-		cface[i] = make_int4(cf[0], cf[1], cf[2], cf[3]);
-		cnbr[i] = make_int4(cn[0], cn[1], cn[2], cn[3]);
-		crev[i] = make_int4(rv[0], rv[1], rv[2], rv[3]);
-	}
-	for (int f = 0; f < nf; f++) {
-		flr[f] = make_int2(h.face_l[f], h.face_r[f]);
-		fslot[f] = make_int2(h.face_sl[f], h.face_sr[f]);
-		fgeo[f] = d4{h.fnorm[3 * f], h.fnorm[3 * f + 1], h.fnorm[3 * f + 2], 0.0};
-		fcen[f] = make_double2(h.fc[2 * f], h.fc[2 * f + 1]);
-	}
-	for (int f = 0; f < nb; f++) gcen[f] = make_double2(h.gc[2 * f], h.gc[2 * f + 1]);
+	d.nelem = h.nelem; d.nbface = h.nbface; d.naface = h.naface; d.ncolors = h.ncolors;
+	const MeshArrays a = mesh_arrays(h);
+	const std::vector<double2> &cc = a.cc, &fcen = a.fcen, &gcen = a.gcen;
+	const std::vector<double> &area = a.area, &iarea = a.iarea;
+	const std::vector<int4> &cface = a.cface, &cnbr = a.cnbr, &crev = a.crev;
+	const std::vector<int2> &flr = a.flr, &fslot = a.fslot;
+	const std::vector<d4> &fgeo = a.fgeo;
 	cudaError_t e = cudaSuccess;
 	std::vector<void *> *own = nullptr;
 	if (!e) e = dupload(&d.cc, cc, own);
@@ -301,52 +272,10 @@ fv_status fv_disc_create(fv_mesh *m, const fv_physics_cfg *phys, int batch, cons
 	if (st) { delete D; return st; }
 	// per-face / per-cell precomputation
 	const int ne = h.nelem, nf = h.naface, nb = h.nbface;
-	std::vector<double2> fwdr(nf), fggw(nf);
-	std::vector<d4> fvis(nf), vinv(ne);
-	std::vector<double> veps2(ne, 0.0);
-	std::vector<double> V(4 * (size_t)ne, 0.0);
-	for (int f = 0; f < nf; f++) {
-		const int L = h.face_l[f];
-		const double xl = h.cc[2 * L], yl = h.cc[2 * L + 1];
-		const double xr = f < nb ? h.gc[2 * f] : h.cc[2 * h.face_r[f]];
-		const double yr = f < nb ? h.gc[2 * f + 1] : h.cc[2 * h.face_r[f] + 1];
-		// weighted least squares (agradientschemes.cpp:219-317)
-		const double dx = xl - xr, dy = yl - yr;
-		const double w2 = 1.0 / (dx * dx + dy * dy);
-		fwdr[f] = make_double2(w2 * dx, w2 * dy);
-		const double a = w2 * dx * dx, bb = w2 * dx * dy, c = w2 * dy * dy;
-		V[4 * L] += a; V[4 * L + 1] += bb; V[4 * L + 2] += bb; V[4 * L + 3] += c;
-		if (f >= nb) {
-			const int R = h.face_r[f];
-			V[4 * R] += a; V[4 * R + 1] += bb; V[4 * R + 2] += bb; V[4 * R + 3] += c;
-		}
-		// Green-Gauss inverse-distance weights (agradientschemes.cpp:62-216)
-		const double mx = h.fc[2 * f], my = h.fc[2 * f + 1];
-		const double dL = 1.0 / std::sqrt((mx - xl) * (mx - xl) + (my - yl) * (my - yl));
-		const double dR = 1.0 / std::sqrt((mx - xr) * (mx - xr) + (my - yr) * (my - yr));
-		const double len = h.fnorm[3 * f + 2];
-		fggw[f] = make_double2(dL / (dL + dR) * len, dR / (dL + dR) * len);
-		// viscous face geometry (aspatial.cpp:172-205)
-		const double ex = xr - xl, ey = yr - yl, dist = std::sqrt(ex * ex + ey * ey);
-		fvis[f] = d4{ex / dist, ey / dist, 1.0 / dist, dist};
-	}
-	for (int i = 0; i < ne; i++) {
-		const double a = V[4 * i], bb = V[4 * i + 1], c = V[4 * i + 2], dd = V[4 * i + 3];
-		const double det = a * dd - bb * c;
-		vinv[i] = d4{dd / det, -bb / det, -c / det, a / det};
-	}
-	if (num->reconstruction == FV_REC_VENKATAKRISHNAN) {
-		// characteristic length = longest cell edge (limitedlinearreconstruction.cpp:180-205)
-		for (int i = 0; i < ne; i++) {
-			double l2 = 0;
-			for (int j = 0; j < h.nnode[i]; j++) {
-				const int p = h.inpoel[4 * i + j], q = h.inpoel[4 * i + (j + 1) % h.nnode[i]];
-				const double ex = h.coords[2 * p] - h.coords[2 * q], ey = h.coords[2 * p + 1] - h.coords[2 * q + 1];
-				l2 = std::max(l2, ex * ex + ey * ey);
-			}
-			veps2[i] = std::pow(num->limiter_param * std::sqrt(l2), 3);
-		}
-	}
+	const DiscArrays da = disc_arrays(h, num->reconstruction == FV_REC_VENKATAKRISHNAN, num->limiter_param);
+	const std::vector<double2> &fwdr = da.fwdr, &fggw = da.fggw;
+	const std::vector<d4> &fvis = da.fvis, &vinv = da.vinv;
+	const std::vector<double> &veps2 = da.veps2;
 	DiscDev &d = D->d;
 	std::memset(&d, 0, sizeof(d));
 	d.nelem = ne; d.nbface = nb; d.naface = nf; d.batch = batch;

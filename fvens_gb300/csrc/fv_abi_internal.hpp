@@ -4,6 +4,13 @@
 #include "../../include/fvens_gb300.h"
 #include "fv_core.cuh"
 
+struct fv_mesh : fvg::fv_mesh_impl {};
+struct fv_disc : fvg::fv_disc_impl {};
+struct fv_matrix {
+	fvg::BlockMatrix A;
+	fv_disc *owner = nullptr;
+};
+
 namespace fvg {
 void set_error(const std::string &s);
 void count_launches(long long n);

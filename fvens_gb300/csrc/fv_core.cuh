@@ -4,7 +4,7 @@
 //   cells (RCM order): centroid double2, area, 1/area; per cell an int4 of
 //     encoded faces ((face << 1) | side, side 1 = cell is the right cell,
 //     -1 = no fourth edge) and an int4 of neighbours (cell index, or
-//     -1 - ib for the ghost of boundary face ib, -2 none), both in local-edge
+//     -1 - ib for the ghost of boundary face ib, NO_EDGE none), both in local-edge
 //     order so a warp reads its cells' stencils with 16-byte loads.
 //   faces (boundary faces first): int2 (left, right | -1-ib), double4
 //     (nx, ny, len, 0), face centre double2; per-face gradient weights.
@@ -23,6 +23,10 @@
 #include "fv_mesh.hpp"
 
 namespace fvg {
+
+/* marker of the unused fourth edge of a triangle in per-cell neighbour lists
+ * (distinct from every boundary-ghost code -1 - ib) */
+constexpr int NO_EDGE = -2147483647 - 1;
 
 struct __align__(32) d4 { double x, y, z, w; };
 struct __align__(16) f4 { float x, y, z, w; };
@@ -72,7 +76,12 @@ struct DiscDev {
 	// configuration
 	int flux, jflux, gradscheme, recon, order2, viscous, constvisc;
 	double limparam;
+	// batch members to skip (set by the steady solver once a member has
+	// converged or failed); NULL = evaluate every member
+	const int *active;
 };
+
+__device__ __forceinline__ bool skip_member(const DiscDev &D, int b) { return D.active && !D.active[b]; }
 
 /* Scratch of one residual evaluation (per batch member slices). */
 struct ResidualWork {

@@ -1,0 +1,678 @@
+// Preconditioners, block SpMV and batched FGMRES; see fv_linalg.cuh.
+#include <algorithm>
+#include <cmath>
+#include "fv_linalg.cuh"
+
+namespace fvg {
+
+namespace {
+
+constexpr int BS = 128;
+constexpr int RBS = 256;  // reduction block size
+
+template <class R>
+__device__ __forceinline__ void load_blk(const R *p, R *b)
+{
+	if (sizeof(R) == 4) {
+		const float4 *q = reinterpret_cast<const float4 *>(p);
+		for (int k = 0; k < 4; k++) {
+			const float4 v = q[k];
+			b[4 * k] = R(v.x); b[4 * k + 1] = R(v.y); b[4 * k + 2] = R(v.z); b[4 * k + 3] = R(v.w);
+		}
+	} else {
+		const double2 *q = reinterpret_cast<const double2 *>(p);
+		for (int k = 0; k < 8; k++) {
+			const double2 v = q[k];
+			b[2 * k] = R(v.x); b[2 * k + 1] = R(v.y);
+		}
+	}
+}
+
+template <class R>
+__device__ __forceinline__ void store_blk(R *p, const R *b)
+{
+	if (sizeof(R) == 4) {
+		float4 *q = reinterpret_cast<float4 *>(p);
+		for (int k = 0; k < 4; k++) q[k] = make_float4(float(b[4 * k]), float(b[4 * k + 1]), float(b[4 * k + 2]), float(b[4 * k + 3]));
+	} else {
+		double2 *q = reinterpret_cast<double2 *>(p);
+		for (int k = 0; k < 8; k++) q[k] = make_double2(double(b[2 * k]), double(b[2 * k + 1]));
+	}
+}
+
+template <class R>
+__device__ __forceinline__ void mv(const R *a, const R *x, R *y)
+{
+	for (int i = 0; i < 4; i++) y[i] = a[4 * i] * x[0] + a[4 * i + 1] * x[1] + a[4 * i + 2] * x[2] + a[4 * i + 3] * x[3];
+}
+
+template <class R>
+__device__ __forceinline__ void mm(const R *a, const R *b, R *c)
+{
+	for (int i = 0; i < 4; i++)
+		for (int j = 0; j < 4; j++)
+			c[4 * i + j] = a[4 * i] * b[j] + a[4 * i + 1] * b[4 + j] + a[4 * i + 2] * b[8 + j] + a[4 * i + 3] * b[12 + j];
+}
+
+/* 4x4 inverse by Gauss-Jordan with partial pivoting; false if singular */
+template <class R>
+__device__ __forceinline__ bool inv4(const R *a, R *out)
+{
+	R m[4][8];
+	for (int i = 0; i < 4; i++)
+		for (int j = 0; j < 4; j++) {
+			m[i][j] = a[4 * i + j];
+			m[i][4 + j] = i == j ? R(1) : R(0);
+		}
+	for (int c = 0; c < 4; c++) {
+		int p = c;
+		R best = fabs(m[c][c]);
+		for (int r = c + 1; r < 4; r++)
+			if (fabs(m[r][c]) > best) { best = fabs(m[r][c]); p = r; }
+		if (!(best > R(0))) return false;
+		if (p != c)
+			for (int j = 0; j < 8; j++) { const R t = m[p][j]; m[p][j] = m[c][j]; m[c][j] = t; }
+		const R iv = R(1) / m[c][c];
+		for (int j = 0; j < 8; j++) m[c][j] *= iv;
+		for (int r = 0; r < 4; r++)
+			if (r != c) {
+				const R f = m[r][c];
+				for (int j = 0; j < 8; j++) m[r][j] -= f * m[c][j];
+			}
+	}
+	for (int i = 0; i < 4; i++)
+		for (int j = 0; j < 4; j++) out[4 * i + j] = m[i][4 + j];
+	return true;
+}
+
+__device__ __forceinline__ bool member_off(const int *active, int b) { return active && !active[b]; }
+
+// ------------------------------ preconditioners -------------------------------
+
+/* inverted diagonal blocks in colour order (Jacobi, SGS); SGS also copies the
+ * matrix rows into colour order */
+template <class R, class RA>
+__global__ void __launch_bounds__(BS) k_diag_setup(int nelem, const RA *__restrict__ A, const int *__restrict__ pos_cell,
+                                                   R *__restrict__ F, R *__restrict__ Dinv, int copy_rows,
+                                                   int *err, const int *active)
+{
+	const int b = blockIdx.y;
+	const int p = blockIdx.x * BS + threadIdx.x;
+	if (p >= nelem || member_off(active, b)) return;
+	const int i = pos_cell[p];
+	const size_t N = nelem;
+	const RA *Ab = A + (size_t)b * 5 * N * 16;
+	R blk[16], inv[16];
+	RA tmp[16];
+	load_blk(Ab + (size_t)i * 16, tmp);
+	for (int q = 0; q < 16; q++) blk[q] = R(tmp[q]);
+	if (!inv4(blk, inv)) { atomicOr(err, 1); for (int q = 0; q < 16; q++) inv[q] = R(0); }
+	store_blk(Dinv + ((size_t)b * N + p) * 16, inv);
+	if (copy_rows) {
+		R *Fb = F + (size_t)b * 5 * N * 16;
+		for (int s = 0; s < 5; s++) {
+			load_blk(Ab + ((size_t)s * N + i) * 16, tmp);
+			for (int q = 0; q < 16; q++) blk[q] = R(tmp[q]);
+			store_blk(Fb + ((size_t)s * N + p) * 16, blk);
+		}
+	}
+}
+
+/* block ILU(0) of the rows of one colour (IKJ, no fill, colour elimination order) */
+template <class R, class RA>
+__global__ void __launch_bounds__(BS) k_ilu_colour(int nelem, int p0, int p1, const RA *__restrict__ A,
+                                                   const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
+                                                   const int4 *__restrict__ pnbrpos, R *__restrict__ F,
+                                                   R *__restrict__ Dinv, int *err, const int *active)
+{
+	const int b = blockIdx.y;
+	const int p = p0 + blockIdx.x * BS + threadIdx.x;
+	if (p >= p1 || member_off(active, b)) return;
+	const size_t N = nelem;
+	const int i = pos_cell[p];
+	const RA *Ab = A + (size_t)b * 5 * N * 16;
+	R *Fb = F + (size_t)b * 5 * N * 16;
+	R *Db = Dinv + (size_t)b * N * 16;
+	const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
+	const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+	const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+	R row[5][16];
+	for (int s = 0; s < 5; s++) {
+		RA tmp[16];
+		load_blk(Ab + ((size_t)s * N + i) * 16, tmp);
+		for (int q = 0; q < 16; q++) row[s][q] = R(tmp[q]);
+	}
+	// lower neighbours in ascending elimination position
+	int ord[4], nl = 0;
+	for (int j = 0; j < 4; j++)
+		if (nbp[j] >= 0 && nbp[j] < p) ord[nl++] = j;
+	for (int a = 1; a < nl; a++)
+		for (int c = a; c > 0 && nbp[ord[c]] < nbp[ord[c - 1]]; c--) { const int t = ord[c]; ord[c] = ord[c - 1]; ord[c - 1] = t; }
+	for (int a = 0; a < nl; a++) {
+		const int jk = ord[a];
+		const int pk = nbp[jk];
+		R dk[16], L[16];
+		load_blk(Db + (size_t)pk * 16, dk);
+		mm(row[1 + jk], dk, L);
+		for (int q = 0; q < 16; q++) row[1 + jk][q] = L[q];
+		// row k's neighbours (cells) to locate U_kj
+		const int4 kn4 = pnbr[pk];
+		const int kn[4] = {kn4.x, kn4.y, kn4.z, kn4.w};
+		// columns j of row i after k: the diagonal (j = i) and upper-position neighbours
+		for (int s = 0; s < 5; s++) {
+			int colcell, colpos;
+			if (s == 0) { colcell = i; colpos = p; }
+			else { colcell = nbc[s - 1]; colpos = nbp[s - 1]; }
+			if (colpos < 0 || colpos <= pk) continue;
+			int ks = -1;
+			for (int t = 0; t < 4; t++)
+				if (kn[t] == colcell) ks = t;
+			if (ks < 0) continue;
+			R ukj[16], prod[16];
+			load_blk(Fb + ((size_t)(1 + ks) * N + pk) * 16, ukj);
+			mm(L, ukj, prod);
+			for (int q = 0; q < 16; q++) row[s][q] -= prod[q];
+		}
+	}
+	R inv[16];
+	if (!inv4(row[0], inv)) { atomicOr(err, 1); for (int q = 0; q < 16; q++) inv[q] = R(0); }
+	store_blk(Db + (size_t)p * 16, inv);
+	for (int s = 0; s < 5; s++) store_blk(Fb + ((size_t)s * N + p) * 16, row[s]);
+}
+
+/* forward sweep of one colour: y_p = r_i - sum_{lower} L y  (ILU) or
+ * Dinv (r_i - sum_{lower} A y) (SGS) */
+template <class R>
+__global__ void __launch_bounds__(BS) k_fwd(int nelem, int p0, int p1, int sgs, const double *__restrict__ r,
+                                            const int *__restrict__ pos_cell, const int4 *__restrict__ pnbrpos,
+                                            const R *__restrict__ F, const R *__restrict__ Dinv, R *__restrict__ y,
+                                            const int *active)
+{
+	const int b = blockIdx.y;
+	const int p = p0 + blockIdx.x * BS + threadIdx.x;
+	if (p >= p1 || member_off(active, b)) return;
+	const size_t N = nelem;
+	const int i = pos_cell[p];
+	const double4 *rb = reinterpret_cast<const double4 *>(r + (size_t)b * N * 4);
+	const double4 rv = rb[i];
+	R s[4] = {R(rv.x), R(rv.y), R(rv.z), R(rv.w)};
+	const int4 np4 = pnbrpos[p];
+	const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+	const R *Fb = F + (size_t)b * 5 * N * 16;
+	const R *yb = y + (size_t)b * N * 4;
+	for (int j = 0; j < 4; j++) {
+		if (nbp[j] < 0 || nbp[j] >= p) continue;
+		R blk[16], t[4];
+		load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
+		const R yy[4] = {yb[4 * (size_t)nbp[j]], yb[4 * (size_t)nbp[j] + 1], yb[4 * (size_t)nbp[j] + 2], yb[4 * (size_t)nbp[j] + 3]};
+		mv(blk, yy, t);
+		for (int q = 0; q < 4; q++) s[q] -= t[q];
+	}
+	R *yo = y + ((size_t)b * N + p) * 4;
+	if (sgs) {
+		R d[16], t[4];
+		load_blk(Dinv + ((size_t)b * N + p) * 16, d);
+		mv(d, s, t);
+		for (int q = 0; q < 4; q++) yo[q] = t[q];
+	} else {
+		for (int q = 0; q < 4; q++) yo[q] = s[q];
+	}
+}
+
+/* backward sweep of one colour: z_i = Dinv (y_p - sum_{upper} U z) (ILU) or
+ * y_p - Dinv sum_{upper} A z (SGS) */
+template <class R>
+__global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, const int *__restrict__ pos_cell,
+                                            const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
+                                            const R *__restrict__ F, const R *__restrict__ Dinv, const R *__restrict__ y,
+                                            double *__restrict__ z, const int *active)
+{
+	const int b = blockIdx.y;
+	const int p = p0 + blockIdx.x * BS + threadIdx.x;
+	if (p >= p1 || member_off(active, b)) return;
+	const size_t N = nelem;
+	const int i = pos_cell[p];
+	const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
+	const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+	const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+	const R *Fb = F + (size_t)b * 5 * N * 16;
+	double *zb = z + (size_t)b * N * 4;
+	R t[4] = {R(0), R(0), R(0), R(0)};
+	for (int j = 0; j < 4; j++) {
+		if (nbp[j] < 0 || nbp[j] <= p) continue;
+		R blk[16], u[4];
+		load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
+		const double4 zz = reinterpret_cast<const double4 *>(zb)[nbc[j]];
+		const R zv[4] = {R(zz.x), R(zz.y), R(zz.z), R(zz.w)};
+		mv(blk, zv, u);
+		for (int q = 0; q < 4; q++) t[q] += u[q];
+	}
+	const R *yp = y + ((size_t)b * N + p) * 4;
+	R d[16], out[4];
+	load_blk(Dinv + ((size_t)b * N + p) * 16, d);
+	if (sgs) {
+		R u[4];
+		mv(d, t, u);
+		for (int q = 0; q < 4; q++) out[q] = yp[q] - u[q];
+	} else {
+		const R v[4] = {yp[0] - t[0], yp[1] - t[1], yp[2] - t[2], yp[3] - t[3]};
+		mv(d, v, out);
+	}
+	reinterpret_cast<double4 *>(zb)[i] = make_double4(double(out[0]), double(out[1]), double(out[2]), double(out[3]));
+}
+
+template <class R>
+__global__ void __launch_bounds__(BS) k_jacobi_apply(int nelem, const double *__restrict__ r, const int *__restrict__ cell_pos,
+                                                     const R *__restrict__ Dinv, double *__restrict__ z, const int *active)
+{
+	const int b = blockIdx.y;
+	const int i = blockIdx.x * BS + threadIdx.x;
+	if (i >= nelem || member_off(active, b)) return;
+	const size_t N = nelem;
+	const double4 rv = reinterpret_cast<const double4 *>(r + (size_t)b * N * 4)[i];
+	const R s[4] = {R(rv.x), R(rv.y), R(rv.z), R(rv.w)};
+	R d[16], o[4];
+	load_blk(Dinv + ((size_t)b * N + cell_pos[i]) * 16, d);
+	mv(d, s, o);
+	reinterpret_cast<double4 *>(z + (size_t)b * N * 4)[i] = make_double4(double(o[0]), double(o[1]), double(o[2]), double(o[3]));
+}
+
+__global__ void k_copy(size_t n, const double *__restrict__ a, double *__restrict__ b, const int *active, size_t per)
+{
+	const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n) return;
+	if (active && !active[t / per]) return;
+	b[t] = a[t];
+}
+
+// ---------------------------------- SpMV ---------------------------------------
+
+template <class R>
+__global__ void __launch_bounds__(BS) k_spmv(int nelem, const R *__restrict__ A, const int4 *__restrict__ cnbr,
+                                             const double *__restrict__ x, double *__restrict__ y, const int *active)
+{
+	const int b = blockIdx.y;
+	const int i = blockIdx.x * BS + threadIdx.x;
+	if (i >= nelem || member_off(active, b)) return;
+	const size_t N = nelem;
+	const R *Ab = A + (size_t)b * 5 * N * 16;
+	const double4 *xb = reinterpret_cast<const double4 *>(x + (size_t)b * N * 4);
+	const int4 c4 = cnbr[i];
+	const int cols[5] = {i, c4.x, c4.y, c4.z, c4.w};
+	R acc[4] = {R(0), R(0), R(0), R(0)};
+	for (int s = 0; s < 5; s++) {
+		if (cols[s] < 0) continue;
+		R blk[16], t[4];
+		load_blk(Ab + ((size_t)s * N + i) * 16, blk);
+		const double4 xv = xb[cols[s]];
+		const R xx[4] = {R(xv.x), R(xv.y), R(xv.z), R(xv.w)};
+		mv(blk, xx, t);
+		for (int q = 0; q < 4; q++) acc[q] += t[q];
+	}
+	reinterpret_cast<double4 *>(y + (size_t)b * N * 4)[i] = make_double4(double(acc[0]), double(acc[1]), double(acc[2]), double(acc[3]));
+}
+
+// ------------------------------ Krylov kernels ---------------------------------
+
+/* partial dot products: part[b][slot][blk] = sum over this block's share of a.b
+ * (a = V_i when vbase != NULL: vector index i = blockIdx.z) */
+__global__ void __launch_bounds__(RBS) k_dot_partial(int n, int nblk, const double *__restrict__ a, size_t astride,
+                                                     size_t aistride, const double *__restrict__ w, size_t wstride,
+                                                     double *__restrict__ part, int slot0, int pstride,
+                                                     const int *active)
+{
+	const int b = blockIdx.y, i = blockIdx.z;
+	if (member_off(active, b)) return;
+	const double *av = a + (size_t)b * astride + (size_t)i * aistride;
+	const double *wv = w + (size_t)b * wstride;
+	double s = 0;
+	for (int e = blockIdx.x * RBS + threadIdx.x; e < n; e += nblk * RBS) s += av[e] * wv[e];
+	__shared__ double sh[RBS];
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = RBS / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) part[((size_t)b * pstride + slot0 + i) * nblk + blockIdx.x] = sh[0];
+}
+
+__device__ __forceinline__ double block_sum(const double *p, int nblk)
+{
+	// deterministic fixed-order sum by one warp
+	double s = 0;
+	for (int k = threadIdx.x; k < nblk; k += 32) s += p[k];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+	return __shfl_sync(0xffffffffu, s, 0);
+}
+
+/* init: bnorm, target, g, flags; x := 0 */
+__global__ void k_gm_init(Krylov K, int nblk, double rtol, const int *member_active)
+{
+	const int b = blockIdx.x;
+	const double bn = sqrt(block_sum(K.part + (size_t)b * (K.restart + 2) * nblk, nblk));
+	if (threadIdx.x == 0) {
+		double *sc = K.scal + 8 * b;
+		sc[0] = bn;
+		sc[1] = rtol * bn;
+		sc[3] = bn > 0 ? 1.0 / bn : 0.0;
+		const bool on = (!member_active || member_active[b]) && bn > 0;
+		K.active[b] = on ? 1 : 0;
+		K.iters[b] = 0;
+		K.kdone[b] = 0;
+		double *g = K.g + (size_t)b * (K.restart + 1);
+		for (int k = 0; k <= K.restart; k++) g[k] = 0;
+		g[0] = bn;
+	}
+}
+
+/* v = scal * a for active members (scal = K.scal[b][idx]) */
+__global__ void k_scale(size_t n, const double *__restrict__ a, size_t astride, double *__restrict__ v, size_t vstride,
+                        const double *__restrict__ scal, int idx, const int *active, int zero_x_of, double *x)
+{
+	const int b = blockIdx.y;
+	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= n) return;
+	if (zero_x_of && x) x[(size_t)b * n + e] = 0.0;
+	if (member_off(active, b)) return;
+	v[(size_t)b * vstride + e] = scal[8 * b + idx] * a[(size_t)b * astride + e];
+}
+
+/* h_i (i <= j) from partials into H[:, j] */
+__global__ void k_reduce_h(Krylov K, int j, int nblk)
+{
+	const int b = blockIdx.x;
+	if (!K.active[b]) return;
+	for (int i = 0; i <= j; i++) {
+		const double h = block_sum(K.part + ((size_t)b * (K.restart + 2) + i) * nblk, nblk);
+		if (threadIdx.x == 0) K.H[(size_t)b * (K.restart + 1) * K.restart + (size_t)i * K.restart + j] = h;
+	}
+}
+
+/* w -= sum_{i<=j} h_i v_i; partial ||w||^2 into part slot restart+1 */
+__global__ void __launch_bounds__(RBS) k_cgs_update(Krylov K, int j, int nblk)
+{
+	const int b = blockIdx.y;
+	if (!K.active[b]) return;
+	const int n = K.n;
+	const size_t vstep = (size_t)K.batch * n;  // V layout [vector][member][n]
+	const double *Vb = K.V + (size_t)b * n;
+	const double *Hb = K.H + (size_t)b * (K.restart + 1) * K.restart;
+	double *wb = K.w + (size_t)b * n;
+	double s = 0;
+	for (int e = blockIdx.x * RBS + threadIdx.x; e < n; e += nblk * RBS) {
+		double x = wb[e];
+		for (int i = 0; i <= j; i++) x -= Hb[(size_t)i * K.restart + j] * Vb[(size_t)i * vstep + e];
+		wb[e] = x;
+		s += x * x;
+	}
+	__shared__ double sh[RBS];
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = RBS / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) K.part[((size_t)b * (K.restart + 2) + K.restart + 1) * nblk + blockIdx.x] = sh[0];
+}
+
+/* Givens rotation of column j, residual estimate, convergence */
+__global__ void k_givens(Krylov K, int j, int nblk, int maxit)
+{
+	const int b = blockIdx.x;
+	if (!K.active[b]) return;
+	const double hn = sqrt(block_sum(K.part + ((size_t)b * (K.restart + 2) + K.restart + 1) * nblk, nblk));
+	if (threadIdx.x != 0) return;
+	const int m = K.restart;
+	double *H = K.H + (size_t)b * (m + 1) * m;
+	double *cs = K.cs + (size_t)b * (m + 1), *sn = K.sn + (size_t)b * (m + 1), *g = K.g + (size_t)b * (m + 1);
+	double *sc = K.scal + 8 * b;
+	H[(size_t)(j + 1) * m + j] = hn;
+	for (int i = 0; i < j; i++) {
+		const double a = H[(size_t)i * m + j], c = H[(size_t)(i + 1) * m + j];
+		H[(size_t)i * m + j] = cs[i] * a + sn[i] * c;
+		H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+	}
+	const double a = H[(size_t)j * m + j], c = H[(size_t)(j + 1) * m + j];
+	const double den = sqrt(a * a + c * c);
+	cs[j] = a / den;
+	sn[j] = c / den;
+	H[(size_t)j * m + j] = den;
+	H[(size_t)(j + 1) * m + j] = 0.0;
+	g[j + 1] = -sn[j] * g[j];
+	g[j] = cs[j] * g[j];
+	K.iters[b] = j + 1;
+	K.kdone[b] = j + 1;
+	sc[2] = hn > 0 ? 1.0 / hn : 0.0;
+	sc[4] = fabs(g[j + 1]);
+	if (fabs(g[j + 1]) <= sc[1] || hn == 0.0 || j + 1 >= maxit) K.active[b] = 0;
+}
+
+/* y = H^{-1} g (upper triangular kdone x kdone), stored in g */
+__global__ void k_backsolve(Krylov K, const int *member_active)
+{
+	const int b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b >= K.batch) return;
+	if (member_active && !member_active[b]) return;
+	const int m = K.restart, k = K.kdone[b];
+	const double *H = K.H + (size_t)b * (m + 1) * m;
+	double *g = K.g + (size_t)b * (m + 1);
+	for (int i = k - 1; i >= 0; i--) {
+		double s = g[i];
+		for (int jj = i + 1; jj < k; jj++) s -= H[(size_t)i * m + jj] * g[jj];
+		g[i] = s / H[(size_t)i * m + i];
+	}
+}
+
+/* x += sum_i y_i z_i */
+__global__ void k_update_x(Krylov K, double *__restrict__ x, const int *member_active)
+{
+	const int b = blockIdx.y;
+	if (member_active && !member_active[b]) return;
+	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= (size_t)K.n) return;
+	const int k = K.kdone[b];
+	const double *g = K.g + (size_t)b * (K.restart + 1);
+	const size_t zstep = (size_t)K.batch * K.n;  // Z layout [vector][member][n]
+	const double *Zb = K.Z + (size_t)b * K.n;
+	double s = x[(size_t)b * K.n + e];
+	for (int i = 0; i < k; i++) s += g[i] * Zb[(size_t)i * zstep + e];
+	x[(size_t)b * K.n + e] = s;
+}
+
+template <class R>
+cudaError_t precond_setup_t(Precond &P, int *err, const int *active, cudaStream_t s, int *nk)
+{
+	const int N = P.nelem, B = P.batch;
+	R *F = (R *)P.F, *D = (R *)P.Dinv;
+	auto go = [&](const auto *A) {
+		if (P.type == PC_JACOBI || P.type == PC_SGS) {
+			k_diag_setup<R><<<dim3((N + BS - 1) / BS, B), BS, 0, s>>>(N, A, P.pos_cell, F, D, P.type == PC_SGS, err, active);
+			(*nk)++;
+		} else if (P.type == PC_ILU0) {
+			for (int c = 0; c < P.ncolors; c++) {
+				const int p0 = P.cptr[c], p1 = P.cptr[c + 1];
+				if (p1 <= p0) continue;
+				k_ilu_colour<R><<<dim3((p1 - p0 + BS - 1) / BS, B), BS, 0, s>>>(N, p0, p1, A, P.pos_cell, P.pnbr,
+				                                                              P.pnbrpos, F, D, err, active);
+				(*nk)++;
+			}
+		}
+	};
+	if (P.A->prec == 4) go((const float *)P.A->val);
+	else go((const double *)P.A->val);
+	return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const int *active, cudaStream_t s, int *nk)
+{
+	const int N = P.nelem, B = P.batch;
+	const R *F = (const R *)P.F, *D = (const R *)P.Dinv;
+	R *y = (R *)P.y;
+	if (P.type == PC_NONE) {
+		const size_t n = (size_t)B * N * 4;
+		k_copy<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, r, z, active, (size_t)N * 4);
+		(*nk)++;
+	} else if (P.type == PC_JACOBI) {
+		k_jacobi_apply<R><<<dim3((N + BS - 1) / BS, B), BS, 0, s>>>(N, r, P.cell_pos, D, z, active);
+		(*nk)++;
+	} else {
+		const int sgs = P.type == PC_SGS;
+		for (int c = 0; c < P.ncolors; c++) {
+			const int p0 = P.cptr[c], p1 = P.cptr[c + 1];
+			if (p1 <= p0) continue;
+			k_fwd<R><<<dim3((p1 - p0 + BS - 1) / BS, B), BS, 0, s>>>(N, p0, p1, sgs, r, P.pos_cell, P.pnbrpos, F, D, y, active);
+			(*nk)++;
+		}
+		for (int c = P.ncolors - 1; c >= 0; c--) {
+			const int p0 = P.cptr[c], p1 = P.cptr[c + 1];
+			if (p1 <= p0) continue;
+			k_bwd<R><<<dim3((p1 - p0 + BS - 1) / BS, B), BS, 0, s>>>(N, p0, p1, sgs, P.pos_cell, P.pnbr, P.pnbrpos, F, D, y, z, active);
+			(*nk)++;
+		}
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec)
+{
+	P.type = type;
+	P.prec = prec;
+	P.batch = batch;
+	const HostMesh &h = m->h;
+	const int N = h.nelem;
+	P.nelem = N;
+	P.ncolors = h.ncolors;
+	P.cptr = h.color_ptr;
+	std::vector<int> pos_cell = h.color_cells, cell_pos(N);
+	for (int p = 0; p < N; p++) cell_pos[pos_cell[p]] = p;
+	std::vector<int4> pn(N), pp(N);
+	for (int p = 0; p < N; p++) {
+		const int i = pos_cell[p];
+		int a[4], c[4];
+		for (int j = 0; j < 4; j++) {
+			const int nb = j < h.nnode[i] ? h.esuel[4 * i + j] : NO_EDGE;
+			a[j] = nb >= 0 ? nb : -1;
+			c[j] = nb >= 0 ? cell_pos[nb] : -1;
+		}
+		pn[p] = make_int4(a[0], a[1], a[2], a[3]);
+		pp[p] = make_int4(c[0], c[1], c[2], c[3]);
+	}
+	cudaError_t e = cudaSuccess;
+	auto up = [&](void **d, const void *src, size_t bytes) {
+		if (e) return;
+		e = cudaMalloc(d, bytes);
+		if (!e) e = cudaMemcpy(*d, src, bytes, cudaMemcpyHostToDevice);
+	};
+	up((void **)&P.pos_cell, pos_cell.data(), sizeof(int) * N);
+	up((void **)&P.cell_pos, cell_pos.data(), sizeof(int) * N);
+	up((void **)&P.pnbr, pn.data(), sizeof(int4) * N);
+	up((void **)&P.pnbrpos, pp.data(), sizeof(int4) * N);
+	const size_t w = prec;
+	if (!e && (type == PC_SGS || type == PC_ILU0)) e = cudaMalloc(&P.F, (size_t)batch * 5 * N * 16 * w);
+	if (!e) e = cudaMalloc(&P.Dinv, (size_t)batch * N * 16 * w);
+	if (!e) e = cudaMalloc(&P.y, (size_t)batch * N * 4 * w);
+	return e;
+}
+
+void precond_free(Precond &P)
+{
+	void *ps[] = {P.pos_cell, P.cell_pos, P.pnbr, P.pnbrpos, P.F, P.Dinv, P.y};
+	for (void *p : ps)
+		if (p) cudaFree(p);
+	P.pos_cell = nullptr; P.cell_pos = nullptr; P.pnbr = nullptr; P.pnbrpos = nullptr;
+	P.F = nullptr; P.Dinv = nullptr; P.y = nullptr;
+}
+
+cudaError_t precond_setup(Precond &P, int *err, const int *active, cudaStream_t s, int *nk)
+{
+	if (P.type == PC_NONE) return cudaSuccess;
+	return P.prec == 4 ? precond_setup_t<float>(P, err, active, s, nk) : precond_setup_t<double>(P, err, active, s, nk);
+}
+
+cudaError_t precond_apply(const Precond &P, const double *r, double *z, const int *active, cudaStream_t s, int *nk)
+{
+	return P.prec == 4 ? precond_apply_t<float>(P, r, z, active, s, nk) : precond_apply_t<double>(P, r, z, active, s, nk);
+}
+
+cudaError_t block_spmv(const BlockMatrix &A, const int4 *cnbr, const double *x, double *y, const int *active,
+                       cudaStream_t s, int *nk)
+{
+	const dim3 g((A.nelem + BS - 1) / BS, A.batch);
+	if (A.prec == 4) k_spmv<float><<<g, BS, 0, s>>>(A.nelem, (const float *)A.val, cnbr, x, y, active);
+	else k_spmv<double><<<g, BS, 0, s>>>(A.nelem, (const double *)A.val, cnbr, x, y, active);
+	(*nk)++;
+	return cudaGetLastError();
+}
+
+cudaError_t krylov_alloc(Krylov &K, int n, int batch, int restart)
+{
+	K.n = n;
+	K.batch = batch;
+	K.restart = restart;
+	K.nblk = std::max(1, std::min(128, (n + RBS * 8 - 1) / (RBS * 8)));
+	const size_t B = batch;
+	cudaError_t e = cudaSuccess;
+	auto al = [&](void **p, size_t bytes) {
+		if (!e) e = cudaMalloc(p, bytes);
+		if (!e) e = cudaMemset(*p, 0, bytes);
+	};
+	al((void **)&K.V, sizeof(double) * B * (restart + 1) * n);  // [vector][member][n]
+	al((void **)&K.Z, sizeof(double) * B * restart * n);
+	al((void **)&K.w, sizeof(double) * B * n);
+	al((void **)&K.H, sizeof(double) * B * (restart + 1) * restart);
+	al((void **)&K.cs, sizeof(double) * B * (restart + 1));
+	al((void **)&K.sn, sizeof(double) * B * (restart + 1));
+	al((void **)&K.g, sizeof(double) * B * (restart + 1));
+	al((void **)&K.part, sizeof(double) * B * (restart + 2) * K.nblk);
+	al((void **)&K.scal, sizeof(double) * B * 8);
+	al((void **)&K.active, sizeof(int) * B);
+	al((void **)&K.iters, sizeof(int) * B);
+	al((void **)&K.kdone, sizeof(int) * B);
+	return e;
+}
+
+void krylov_free(Krylov &K)
+{
+	void *ps[] = {K.V, K.Z, K.w, K.H, K.cs, K.sn, K.g, K.part, K.scal, K.active, K.iters, K.kdone};
+	for (void *p : ps)
+		if (p) cudaFree(p);
+	K = Krylov();
+}
+
+cudaError_t fgmres_solve(Krylov &K, LinOp &op, const Precond &P, const double *b, double *x, int maxit, double rtol,
+                         const int *member_active, cudaStream_t s, int *nk)
+{
+	const int n = K.n, B = K.batch, m = K.restart, nb = K.nblk;
+	if (maxit > m) maxit = m;  // one cycle (the reference configuration: restart = max_it = 30)
+	const size_t vstep = (size_t)B * n;  // V, Z layout [vector][member][n]
+	const dim3 gr(nb, B);
+	const dim3 ge((unsigned)((n + 255) / 256), B);
+	cudaError_t e;
+	// ||b||, x = 0, v0 = b/||b||
+	k_dot_partial<<<dim3(nb, B, 1), RBS, 0, s>>>(n, nb, b, n, 0, b, n, K.part, 0, m + 2, member_active);
+	k_gm_init<<<B, 32, 0, s>>>(K, nb, rtol, member_active);
+	k_scale<<<ge, 256, 0, s>>>(n, b, n, K.V, n, K.scal, 3, K.active, 1, x);
+	*nk += 3;
+	for (int j = 0; j < maxit; j++) {
+		double *vj = K.V + (size_t)j * vstep;
+		double *zj = K.Z + (size_t)j * vstep;
+		if ((e = precond_apply(P, vj, zj, K.active, s, nk)) != cudaSuccess) return e;
+		if ((e = op.apply(zj, K.w, K.active, s, nk)) != cudaSuccess) return e;
+		k_dot_partial<<<dim3(nb, B, j + 1), RBS, 0, s>>>(n, nb, K.V, n, vstep, K.w, n, K.part, 0, m + 2, K.active);
+		k_reduce_h<<<B, 32, 0, s>>>(K, j, nb);
+		k_cgs_update<<<gr, RBS, 0, s>>>(K, j, nb);
+		k_givens<<<B, 32, 0, s>>>(K, j, nb, maxit);
+		k_scale<<<ge, 256, 0, s>>>(n, K.w, n, K.V + (size_t)(j + 1) * vstep, n, K.scal, 2, K.active, 0, nullptr);
+		*nk += 5;
+	}
+	k_backsolve<<<(B + 31) / 32, 32, 0, s>>>(K, member_active);
+	k_update_x<<<ge, 256, 0, s>>>(K, x, member_active);
+	*nk += 2;
+	return cudaGetLastError();
+}
+
+}  // namespace fvg

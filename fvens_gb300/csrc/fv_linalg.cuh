@@ -1,0 +1,76 @@
+// Block linear algebra of the implicit solve: preconditioners on the stored
+// block Jacobian (point-block Jacobi, multicolour symmetric Gauss-Seidel,
+// multicolour block ILU(0)), block SpMV and batched flexible GMRES.
+//
+// Replaces PETSc's -pc_type pbjacobi / sor / bjacobi+ilu on BAIJ(4) and
+// KSPFGMRES (external to the reference; called from aodesolver.cpp:483).
+// The elimination order of SGS and ILU(0) is the mesh's colour order (cells of
+// colour 0, then colour 1, ...): cells of one colour share no face, so each
+// colour is one fully parallel launch.  The factor is stored in colour order
+// so those launches read contiguous blocks.
+#pragma once
+#include "fv_core.cuh"
+
+namespace fvg {
+
+/* Preconditioner state; PR = float (FP32 sweeps) or double. */
+struct Precond {
+	int type = PC_NONE;
+	int prec = 4;               // 4: FP32 factor, 8: FP64 factor
+	int nelem = 0, batch = 1, ncolors = 0;
+	std::vector<int> cptr;      // colour ranges in the colour-ordered position space
+	int *pos_cell = nullptr;    // [nelem] cell at colour-order position p
+	int *cell_pos = nullptr;    // [nelem] position of cell i
+	int4 *pnbr = nullptr;       // [nelem] neighbours (as cells) of the cell at position p, -1 none
+	int4 *pnbrpos = nullptr;    // [nelem] their positions, -1 none
+	void *F = nullptr;          // [batch][5][nelem][16] factor / copy in colour order
+	void *Dinv = nullptr;       // [batch][nelem][16] inverted (factored) diagonal, colour order
+	void *y = nullptr;          // [batch][nelem][4] intermediate sweep vector, colour order
+	BlockMatrix *A = nullptr;   // source matrix (cell order)
+};
+
+cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec);
+void precond_free(Precond &P);
+/* factorisation / diagonal inversion from P.A; err_flag (device int) is set
+ * non-zero when a diagonal block is singular */
+cudaError_t precond_setup(Precond &P, int *err_flag, const int *active, cudaStream_t s, int *nk);
+/* z = M^{-1} r, FP64 vectors in cell order [batch][nelem][4] */
+cudaError_t precond_apply(const Precond &P, const double *r, double *z, const int *active, cudaStream_t s, int *nk);
+/* y = A x (FP64 vectors, cell order) plus optional diagonal shift diag[cell]*x */
+cudaError_t block_spmv(const BlockMatrix &A, const int4 *cnbr, const double *x, double *y, const int *active,
+                       cudaStream_t s, int *nk);
+
+/* Batched FGMRES(m) workspace (classical Gram-Schmidt, Givens rotations, x0 = 0). */
+struct Krylov {
+	int n = 0;                  // unknowns per member (4 * nelem)
+	int batch = 1, restart = 30;
+	int nblk = 0;               // partial-sum blocks per member
+	double *V = nullptr;        // [restart+1][batch][n]: each basis vector is a batched vector
+	double *Z = nullptr;        // [restart][batch][n]
+	double *w = nullptr;        // [batch][n]
+	double *H = nullptr;        // [batch][(restart+1)*restart]
+	double *cs = nullptr, *sn = nullptr, *g = nullptr;  // [batch][restart+1]
+	double *part = nullptr;     // [batch][restart+2][nblk] partial sums
+	double *scal = nullptr;     // [batch][8]: bnorm, target, hnorm, ...
+	int *active = nullptr;      // [batch] member still iterating
+	int *iters = nullptr;       // [batch] iterations done in this solve
+	int *kdone = nullptr;       // [batch] Krylov dimension used
+};
+
+cudaError_t krylov_alloc(Krylov &K, int n, int batch, int restart);
+void krylov_free(Krylov &K);
+
+/* Operator callback: y = Op(x) for all active members. */
+struct LinOp {
+	virtual cudaError_t apply(const double *x, double *y, const int *active, cudaStream_t s, int *nk) = 0;
+	virtual ~LinOp() {}
+};
+
+/* Solves Op x = b to ||b - Op x|| <= rtol ||b|| (or maxit iterations) for
+ * every member whose member_active flag is set (NULL = all).  The iteration
+ * count per member lands in K.iters.  The sequence of launches does not depend
+ * on data, so it can be captured in a CUDA graph. */
+cudaError_t fgmres_solve(Krylov &K, LinOp &op, const Precond &P, const double *b, double *x, int maxit, double rtol,
+                         const int *member_active, cudaStream_t s, int *nk);
+
+}  // namespace fvg

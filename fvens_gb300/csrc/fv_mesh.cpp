@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <limits>
 #include <numeric>
 #include <sstream>
 #include <unordered_map>
@@ -150,7 +151,7 @@ int HostMesh::build(std::string *err)
 {
 	// ---- edge matching ----
 	std::vector<EdgeRef> e = sorted_edges(nelem, nnode, inpoel);
-	esuel.assign(4 * (size_t)nelem, -2);
+	esuel.assign(4 * (size_t)nelem, std::numeric_limits<int>::min());
 	for (int i = 0; i < nelem; i++)
 		for (int j = 0; j < nnode[i]; j++) esuel[4 * i + j] = kUnmatched;
 	std::vector<int> bnd_edge_idx;  // indices into e of edges with a single owner

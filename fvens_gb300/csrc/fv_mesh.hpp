@@ -30,7 +30,7 @@ struct HostMesh {
 	std::vector<int> face_l, face_r;      // naface; boundary faces: face_r = -1 - ib
 	std::vector<int> face_n0, face_n1;    // naface nodes
 	std::vector<int> face_sl, face_sr;    // local edge index of the face in its left/right cell
-	std::vector<int> esuel;               // nelem x 4: neighbour cell, -1-ib for boundary, -2 unused
+	std::vector<int> esuel;               // nelem x 4: neighbour cell, -1-ib for boundary, INT_MIN unused
 	std::vector<int> elemface;            // nelem x 4
 	// geometry
 	std::vector<double> area;             // nelem

@@ -1,0 +1,668 @@
+// Steady backward-Euler pseudo-time solver on the GPU, and the C ABI of the
+// preconditioner / Krylov / solver handles.
+//
+// Replaces SteadyBackwardEulerSolver::solve (src/ode/aodesolver.cpp:363-638)
+// with expResidualRamp (:110-120), addPseudoTimeTerm (:300-329), the
+// FlowSimpleUpdate relaxation (src/ode/nonlinearrelaxation.cpp:25-38), the
+// matrix-free Jacobian-vector product (src/linalg/alinalg.cpp:143-237) and
+// the KSPSolve call (:483).
+//
+// Every step runs on the device without host decisions: CFL ramp, pseudo-time
+// term, relaxation, residual norm, NaN detection and convergence flags are
+// per-member device scalars, so one step is a fixed launch sequence that is
+// captured once in a CUDA graph and replayed; the host only polls the flags
+// every few steps.  Members of a batch that converged or failed are masked
+// out of every launch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fv_abi_internal.hpp"
+#include "fv_linalg.cuh"
+
+using namespace fvg;
+
+
+namespace fvg {
+
+namespace {
+
+constexpr int BS = 128;
+constexpr int RBS = 256;
+
+/* per-member solver scalars (device) */
+struct StepState {
+	double *res, *resold, *res0, *cfl, *pm;  // [batch]
+	int *step, *status, *active;              // [batch]
+	int *pc_err;                              // [1]
+	double *hist;                             // [maxiter][batch][3]: res, cfl, linear iterations
+	int *linits;                              // [batch] cumulative linear iterations
+};
+
+enum { ST_RUNNING = -1, ST_CONVERGED = 0, ST_NUMERICAL = 3, ST_TOLERANCE = 4, ST_PRECOND = 7 };
+
+/* CFL ramp (expResidualRamp, aodesolver.cpp:110-120) */
+__global__ void k_cfl(int B, StepState S, double cflmin, double cflmax)
+{
+	const int b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b >= B || !S.active[b]) return;
+	const double ratio = S.resold[b] / S.res[b];
+	const double prev = S.cfl[b];
+	double nc = ratio > 1.0 ? prev * pow(ratio, 0.25) : prev * pow(ratio, 0.3);
+	if (nc < cflmin) nc = cflmin;
+	else if (nc > cflmax) nc = cflmax;
+	S.cfl[b] = nc;
+}
+
+/* dtm_i := A_i/(CFL dtm_i); A_ii += dtm_i I (addPseudoTimeTerm, aodesolver.cpp:300-329) */
+template <class R>
+__global__ void __launch_bounds__(BS) k_pseudo_time(int N, const double *__restrict__ area, double *__restrict__ dtm,
+                                                    R *__restrict__ val, StepState S)
+{
+	const int b = blockIdx.y;
+	if (!S.active[b]) return;
+	const int i = blockIdx.x * BS + threadIdx.x;
+	if (i >= N) return;
+	double &d = dtm[(size_t)b * N + i];
+	d = area[i] / (S.cfl[b] * d);
+	R *blk = val + ((size_t)b * 5 * N + i) * 16;
+	const R x = R(d);
+	blk[0] += x; blk[5] += x; blk[10] += x; blk[15] += x;
+}
+
+/* getDeltaPressureFromConserved, aphysics_defs.hpp:67-80 */
+__device__ __forceinline__ double delta_pressure(double g, const double *u, const double *du)
+{
+	double un[4];
+	for (int i = 0; i < 4; i++) un[i] = u[i] + du[i];
+	double dp = 0;
+	for (int i = 2; i < 4; i++)
+		dp -= ((u[i] + un[i]) * (u[0] + un[0]) / 2.0 * du[i] - (un[i] * un[i] + u[i] * u[i]) / 2.0 * du[0]);
+	return (g - 1.0) * (du[3] - 1.0 / (2 * u[0] * un[0]) * dp);
+}
+
+/* u += omega du; partial sums of r_3^2 A for the residual norm (aodesolver.cpp:506-530) */
+__global__ void __launch_bounds__(RBS) k_update(int N, int nblk, double *__restrict__ u, const double *__restrict__ du,
+                                                const double *__restrict__ r, const double *__restrict__ area,
+                                                const Phys *__restrict__ phys, int nl_update, double minf,
+                                                double *__restrict__ part, StepState S)
+{
+	const int b = blockIdx.y;
+	if (!S.active[b]) return;
+	const double g = phys[b].g;
+	double s = 0;
+	for (int i = blockIdx.x * RBS + threadIdx.x; i < N; i += nblk * RBS) {
+		d4 *ub = reinterpret_cast<d4 *>(u + ((size_t)b * N + i) * 4);
+		const d4 dv = *reinterpret_cast<const d4 *>(du + ((size_t)b * N + i) * 4);
+		d4 uv = *ub;
+		double om = 1.0;
+		if (nl_update) {
+			// FlowSimpleUpdate::getLocalRelaxationFactor, nonlinearrelaxation.cpp:25-38
+			const double uu[4] = {uv.x, uv.y, uv.z, uv.w}, dd[4] = {dv.x, dv.y, dv.z, dv.w};
+			const double p = (g - 1.0) * (uu[3] - 0.5 * (uu[1] * uu[1] + uu[2] * uu[2]) / uu[0]);
+			const double dp = fabs(delta_pressure(g, uu, dd)) / p;
+			const double dr = fabs(dd[0]) / uu[0];
+			const double dl = fmax(dp, dr);
+			om = minf;
+			if (dl < 1.0 - minf) om = 1.0 - dl;
+		}
+		uv.x += om * dv.x; uv.y += om * dv.y; uv.z += om * dv.z; uv.w += om * dv.w;
+		*ub = uv;
+		const double r3 = r[((size_t)b * N + i) * 4 + 3];
+		s += r3 * r3 * area[i];
+	}
+	__shared__ double sh[RBS];
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = RBS / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) part[(size_t)b * nblk + blockIdx.x] = sh[0];
+}
+
+/* norm, NaN check, step count, convergence (aodesolver.cpp:516-537, 608-626) */
+__global__ void k_norm(int B, int nblk, const double *__restrict__ part, StepState S, const int *__restrict__ kiters,
+                       double tol, int abs_tol, int maxiter)
+{
+	const int b = blockIdx.x;
+	if (b >= B || !S.active[b]) return;
+	double s = 0;
+	for (int k = threadIdx.x; k < nblk; k += 32) s += part[(size_t)b * nblk + k];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+	if (threadIdx.x != 0) return;
+	const double res = sqrt(s);
+	S.resold[b] = S.res[b];
+	S.res[b] = res;
+	const int step = S.step[b];
+	S.linits[b] += kiters[b];
+	if (S.hist) {
+		double *h = S.hist + ((size_t)step * B + b) * 3;
+		h[0] = res; h[1] = S.cfl[b]; h[2] = kiters[b];
+	}
+	if (*S.pc_err) {
+		S.status[b] = ST_PRECOND;
+		S.active[b] = 0;
+		S.step[b] = step + 1;
+		return;
+	}
+	if (!isfinite(res)) {
+		S.status[b] = ST_NUMERICAL;
+		S.active[b] = 0;
+		S.step[b] = step + 1;
+		return;
+	}
+	if (step == 0) S.res0[b] = res;
+	S.step[b] = step + 1;
+	const bool conv = abs_tol ? (res <= tol) : (res / S.res0[b] <= tol);
+	if (conv) {
+		S.status[b] = ST_CONVERGED;
+		S.active[b] = 0;
+	} else if (step + 1 >= maxiter) {
+		S.status[b] = ST_TOLERANCE;
+		S.active[b] = 0;
+	}
+}
+
+__global__ void k_init(int B, StepState S, const int *__restrict__ mask)
+{
+	const int b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b == 0) *S.pc_err = 0;
+	if (b >= B) return;
+	S.res[b] = 1.0; S.resold[b] = 1.0; S.res0[b] = 1.0; S.cfl[b] = 0.0;
+	S.step[b] = 0; S.linits[b] = 0;
+	const int on = mask ? mask[b] : 1;
+	S.active[b] = on;
+	S.status[b] = on ? ST_RUNNING : ST_CONVERGED;
+}
+
+/* matrix-free product pieces (alinalg.cpp:143-237) */
+__global__ void __launch_bounds__(RBS) k_mf_prep(size_t n, int nblk_unused, const double *__restrict__ u,
+                                                 const double *__restrict__ x, const double *__restrict__ pm,
+                                                 double *__restrict__ aux, double *__restrict__ yg, const int *active)
+{
+	const int b = blockIdx.y;
+	if (active && !active[b]) return;
+	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= n) return;
+	aux[b * n + e] = u[b * n + e] + pm[b] * x[b * n + e];
+	yg[b * n + e] = 0.0;
+}
+
+__global__ void k_mf_pm(int B, int nblk, const double *__restrict__ part, double eps, double *__restrict__ pm,
+                        const int *active)
+{
+	const int b = blockIdx.x;
+	if (b >= B || (active && !active[b])) return;
+	double s = 0;
+	for (int k = threadIdx.x; k < nblk; k += 32) s += part[(size_t)b * nblk + k];
+	for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+	if (threadIdx.x == 0) pm[b] = eps / sqrt(s);
+}
+
+__global__ void k_mf_finish(int N, const double *__restrict__ x, const double *__restrict__ r,
+                            const double *__restrict__ yg, const double *__restrict__ dtm,
+                            const double *__restrict__ pm, double *__restrict__ y, const int *active)
+{
+	const int b = blockIdx.y;
+	if (active && !active[b]) return;
+	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= (size_t)N * 4) return;
+	const size_t k = (size_t)b * N * 4 + e;
+	y[k] = dtm[(size_t)b * N + e / 4] * x[k] + (-yg[k] + r[k]) / pm[b];
+}
+
+__global__ void __launch_bounds__(RBS) k_sq_partial(int n, int nblk, const double *__restrict__ x,
+                                                    double *__restrict__ part, const int *active)
+{
+	const int b = blockIdx.y;
+	if (active && !active[b]) return;
+	const double *xb = x + (size_t)b * n;
+	double s = 0;
+	for (int e = blockIdx.x * RBS + threadIdx.x; e < n; e += nblk * RBS) s += xb[e] * xb[e];
+	__shared__ double sh[RBS];
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = RBS / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) part[(size_t)b * nblk + blockIdx.x] = sh[0];
+}
+
+struct MatrixOp : LinOp {
+	const BlockMatrix *A;
+	const int4 *cnbr;
+	cudaError_t apply(const double *x, double *y, const int *active, cudaStream_t s, int *nk) override
+	{
+		return block_spmv(*A, cnbr, x, y, active, s, nk);
+	}
+};
+
+/* y = dtm x + (R(u + pm x) - R(u)) / pm, pm = eps/||x|| per member */
+struct MatrixFreeOp : LinOp {
+	fv_disc_impl *D;
+	const double *u, *r, *dtm;
+	double *aux, *yg, *pm, *part;
+	int nblk;
+	double eps;
+	cudaError_t apply(const double *x, double *y, const int *active, cudaStream_t s, int *nk) override
+	{
+		const int N = D->d.nelem, B = D->batch;
+		const int n = 4 * N;
+		k_sq_partial<<<dim3(nblk, B), RBS, 0, s>>>(n, nblk, x, part, active);
+		k_mf_pm<<<B, 32, 0, s>>>(B, nblk, part, eps, pm, active);
+		k_mf_prep<<<dim3((n + 255) / 256, B), 256, 0, s>>>((size_t)n, nblk, u, x, pm, aux, yg, active);
+		*nk += 3;
+		const int *saved = D->d.active;
+		D->d.active = active;
+		const int before = D->kernels_launched;
+		cudaError_t e = residual_launch(D, aux, yg, 0, nullptr, s);
+		*nk += D->kernels_launched - before;
+		D->kernels_launched = before;
+		D->d.active = saved;
+		if (e) return e;
+		k_mf_finish<<<dim3((n + 255) / 256, B), 256, 0, s>>>(N, x, r, yg, dtm, pm, y, active);
+		*nk += 1;
+		return cudaGetLastError();
+	}
+};
+
+}  // namespace
+
+}  // namespace fvg
+
+struct fv_precond {
+	Precond P;
+	fv_disc *D = nullptr;
+	fv_matrix *M = nullptr;
+	int *err = nullptr;
+	Krylov K;
+};
+
+struct fv_solver {
+	fv_disc *D = nullptr;
+	fv_solver_cfg cfg;
+	BlockMatrix A;
+	Precond P;
+	Krylov K;
+	StepState S;
+	double *r = nullptr, *du = nullptr, *dtm = nullptr, *part = nullptr;
+	double *aux = nullptr, *yg = nullptr, *mfpart = nullptr;
+	int nblk = 1;
+	std::vector<void *> owned;
+	cudaGraphExec_t exec = nullptr;
+	cudaGraph_t graph = nullptr;
+	bool graph_ready = false;
+	long long kernels_per_step = 0;
+	MatrixOp mop;
+	MatrixFreeOp mfop;
+};
+
+namespace {
+
+template <class T>
+cudaError_t salloc(fv_solver *S, T **p, size_t n)
+{
+	cudaError_t e = cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(n, 1));
+	if (!e) {
+		S->owned.push_back(*p);
+		e = cudaMemset(*p, 0, sizeof(T) * std::max<size_t>(n, 1));
+	}
+	return e;
+}
+
+/* one pseudo-time step for all active members (fixed launch sequence) */
+cudaError_t solver_step(fv_solver *S, double *u, cudaStream_t s, int *nk)
+{
+	fv_disc_impl *D = S->D;
+	const int N = D->d.nelem, B = D->batch;
+	const fv_solver_cfg &c = S->cfg;
+	cudaError_t e;
+	const int *saved = D->d.active;
+	D->d.active = S->S.active;
+	const int kl0 = D->kernels_launched;
+	e = cudaMemsetAsync(S->r, 0, sizeof(double) * 4 * (size_t)N * B, s);
+	if (!e) e = residual_launch(D, u, S->r, 1, S->dtm, s);
+	if (!e) e = jacobian_launch(D, u, S->A, s);
+	*nk += D->kernels_launched - kl0;
+	D->kernels_launched = kl0;
+	D->d.active = saved;
+	if (e) return e;
+	k_cfl<<<(B + 31) / 32, 32, 0, s>>>(B, S->S, c.cfl_min, c.cfl_max);
+	const dim3 gc((N + BS - 1) / BS, B);
+	if (S->A.prec == 4) k_pseudo_time<float><<<gc, BS, 0, s>>>(N, D->d.area, S->dtm, (float *)S->A.val, S->S);
+	else k_pseudo_time<double><<<gc, BS, 0, s>>>(N, D->d.area, S->dtm, (double *)S->A.val, S->S);
+	*nk += 2;
+	if ((e = precond_setup(S->P, S->S.pc_err, S->S.active, s, nk))) return e;
+	LinOp &op = c.matrix_free ? (LinOp &)S->mfop : (LinOp &)S->mop;
+	if ((e = fgmres_solve(S->K, op, S->P, S->r, S->du, c.ksp_maxit, c.ksp_rtol, S->S.active, s, nk))) return e;
+	k_update<<<dim3(S->nblk, B), RBS, 0, s>>>(N, S->nblk, u, S->du, S->r, D->d.area, D->d.phys, c.nl_update,
+	                                           c.min_relax, S->part, S->S);
+	k_norm<<<B, 32, 0, s>>>(B, S->nblk, S->part, S->S, S->K.iters, c.tolerance, c.abs_tolerance, c.max_timesteps);
+	*nk += 2;
+	return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" {
+
+fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, fv_precond **out)
+{
+	if (!D || !M || !out || M->owner != D || type < FV_PC_NONE || type > FV_PC_ILU0) {
+		set_error("invalid argument");
+		return FV_ERR_INVALID;
+	}
+	fv_precond *p = new fv_precond();
+	p->D = D;
+	p->M = M;
+	cudaError_t e = precond_alloc(p->P, D->mesh, D->batch, type, M->A.prec);
+	p->P.A = &M->A;
+	if (!e) e = cudaMalloc(&p->err, sizeof(int));
+	if (!e) e = cudaMemset(p->err, 0, sizeof(int));
+	if (e) {
+		fv_precond_destroy(p);
+		return cuda_status(e, "preconditioner allocation");
+	}
+	*out = p;
+	return FV_OK;
+}
+
+void fv_precond_destroy(fv_precond *p)
+{
+	if (!p) return;
+	precond_free(p->P);
+	krylov_free(p->K);
+	if (p->err) cudaFree(p->err);
+	delete p;
+}
+
+fv_status fv_precond_setup(fv_precond *p)
+{
+	if (!p) { set_error("null argument"); return FV_ERR_INVALID; }
+	int nk = 0;
+	cudaError_t e = cudaMemsetAsync(p->err, 0, sizeof(int), p->D->stream);
+	if (!e) e = precond_setup(p->P, p->err, nullptr, p->D->stream, &nk);
+	count_launches(nk);
+	if (e) return cuda_status(e, "preconditioner setup");
+	int herr = 0;
+	e = cudaMemcpyAsync(&herr, p->err, sizeof(int), cudaMemcpyDeviceToHost, p->D->stream);
+	if (!e) e = cudaStreamSynchronize(p->D->stream);
+	if (e) return cuda_status(e, "preconditioner setup");
+	if (herr) {
+		set_error("singular diagonal block in the preconditioner");
+		return FV_ERR_NUMERICAL;
+	}
+	return FV_OK;
+}
+
+fv_status fv_precond_apply(fv_precond *p, const double *r, double *z)
+{
+	if (!p || !r || !z) { set_error("null argument"); return FV_ERR_INVALID; }
+	int nk = 0;
+	const cudaError_t e = precond_apply(p->P, r, z, nullptr, p->D->stream, &nk);
+	count_launches(nk);
+	return cuda_status(e, "preconditioner apply");
+}
+
+fv_status fv_precond_order(const fv_precond *p, int *order)
+{
+	if (!p || !order) { set_error("null argument"); return FV_ERR_INVALID; }
+	const HostMesh &h = p->D->mesh->h;
+	if (p->P.type == FV_PC_SGS || p->P.type == FV_PC_ILU0) std::memcpy(order, h.color_cells.data(), sizeof(int) * h.nelem);
+	else for (int i = 0; i < h.nelem; i++) order[i] = i;
+	return FV_OK;
+}
+
+fv_status fv_matvec(fv_disc *D, fv_matrix *M, const double *x, double *y)
+{
+	if (!D || !M || !x || !y || M->owner != D) { set_error("invalid argument"); return FV_ERR_INVALID; }
+	int nk = 0;
+	const cudaError_t e = block_spmv(M->A, D->d.cnbr, x, y, nullptr, D->stream, &nk);
+	count_launches(nk);
+	return cuda_status(e, "block spmv");
+}
+
+fv_status fv_ksp_solve(fv_precond *p, const double *b, double *x, int restart, int maxit, double rtol, int *iters)
+{
+	if (!p || !b || !x || restart < 1 || maxit < 1) { set_error("invalid argument"); return FV_ERR_INVALID; }
+	fv_disc *D = p->D;
+	cudaError_t e = cudaSuccess;
+	if (p->K.restart != restart || p->K.n != 4 * D->d.nelem) {
+		krylov_free(p->K);
+		e = krylov_alloc(p->K, 4 * D->d.nelem, D->batch, restart);
+	}
+	if (e) return cuda_status(e, "krylov allocation");
+	MatrixOp op;
+	op.A = &p->M->A;
+	op.cnbr = D->d.cnbr;
+	int nk = 0;
+	e = fgmres_solve(p->K, op, p->P, b, x, maxit, rtol, nullptr, D->stream, &nk);
+	count_launches(nk);
+	if (!e && iters) e = cudaMemcpyAsync(iters, p->K.iters, sizeof(int) * D->batch, cudaMemcpyDeviceToHost, D->stream);
+	if (!e) e = cudaStreamSynchronize(D->stream);
+	return cuda_status(e, "fgmres");
+}
+
+void fv_solver_cfg_default(fv_solver_cfg *c)
+{
+	if (!c) return;
+	std::memset(c, 0, sizeof(*c));
+	c->cfl_min = 10; c->cfl_max = 1000; c->tolerance = 1e-10; c->max_timesteps = 1000; c->abs_tolerance = 1;
+	c->pc_type = FV_PC_ILU0; c->ksp_restart = 30; c->ksp_maxit = 30; c->ksp_rtol = 0.1;
+	c->matrix_free = 0; c->mf_eps = 1e-7; c->nl_update = 0; c->min_relax = 0.2; c->precision = 4;
+	c->check_every = 4; c->use_graph = 1;
+}
+
+fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out)
+{
+	if (!D || !cfg || !out || (cfg->precision != 4 && cfg->precision != 8) || cfg->ksp_restart < 1 ||
+	    cfg->max_timesteps < 1 || cfg->pc_type < FV_PC_NONE || cfg->pc_type > FV_PC_ILU0) {
+		set_error("invalid solver configuration");
+		return FV_ERR_INVALID;
+	}
+	if (D->d.jflux == FV_FLUX_VANLEER || D->d.jflux == FV_FLUX_AUSMPLUS) {
+		set_error("the Jacobian flux has no Jacobian in the reference (VanLeer / AUSM+)");
+		return FV_ERR_UNSUPPORTED;
+	}
+	if (cfg->nl_update && (cfg->min_relax <= 0 || cfg->min_relax > 1.0)) {
+		set_error("Minimum relaxation factor is invalid!");
+		return FV_ERR_INVALID;
+	}
+	fv_solver *S = new fv_solver();
+	S->D = D;
+	S->cfg = *cfg;
+	if (S->cfg.check_every < 1) S->cfg.check_every = 1;
+	const int N = D->d.nelem, B = D->batch;
+	S->A.nelem = N; S->A.batch = B; S->A.prec = cfg->precision;
+	cudaError_t e = cudaSuccess;
+	if (!e) e = salloc(S, (char **)&S->A.val, S->A.nval() * cfg->precision);
+	if (!e) e = salloc(S, &S->A.bdiag, 16 * (size_t)B * std::max(D->d.nbface, 1));
+	if (!e) e = precond_alloc(S->P, D->mesh, B, cfg->pc_type, cfg->precision);
+	S->P.A = &S->A;
+	if (!e) e = krylov_alloc(S->K, 4 * N, B, cfg->ksp_restart);
+	S->nblk = std::max(1, std::min(256, (N + RBS * 8 - 1) / (RBS * 8)));
+	if (!e) e = salloc(S, &S->r, 4 * (size_t)N * B);
+	if (!e) e = salloc(S, &S->du, 4 * (size_t)N * B);
+	if (!e) e = salloc(S, &S->dtm, (size_t)N * B);
+	if (!e) e = salloc(S, &S->part, (size_t)S->nblk * B);
+	if (!e) e = salloc(S, &S->S.res, B);
+	if (!e) e = salloc(S, &S->S.resold, B);
+	if (!e) e = salloc(S, &S->S.res0, B);
+	if (!e) e = salloc(S, &S->S.cfl, B);
+	if (!e) e = salloc(S, &S->S.pm, B);
+	if (!e) e = salloc(S, &S->S.step, B);
+	if (!e) e = salloc(S, &S->S.status, B);
+	if (!e) e = salloc(S, &S->S.active, B);
+	if (!e) e = salloc(S, &S->S.pc_err, 1);
+	if (!e) e = salloc(S, &S->S.linits, B);
+	if (!e) e = salloc(S, &S->S.hist, 3 * (size_t)cfg->max_timesteps * B);
+	if (!e && cfg->matrix_free) {
+		e = salloc(S, &S->aux, 4 * (size_t)N * B);
+		if (!e) e = salloc(S, &S->yg, 4 * (size_t)N * B);
+		if (!e) e = salloc(S, &S->mfpart, (size_t)S->nblk * B);
+	}
+	if (e) {
+		fv_solver_destroy(S);
+		return cuda_status(e, "solver allocation");
+	}
+	S->mop.A = &S->A;
+	S->mop.cnbr = D->d.cnbr;
+	S->mfop.D = D;
+	S->mfop.r = S->r;
+	S->mfop.dtm = S->dtm;
+	S->mfop.aux = S->aux;
+	S->mfop.yg = S->yg;
+	S->mfop.pm = S->S.pm;
+	S->mfop.part = S->mfpart;
+	S->mfop.nblk = S->nblk;
+	S->mfop.eps = cfg->mf_eps;
+	*out = S;
+	return FV_OK;
+}
+
+void fv_solver_destroy(fv_solver *S)
+{
+	if (!S) return;
+	if (S->exec) cudaGraphExecDestroy(S->exec);
+	if (S->graph) cudaGraphDestroy(S->graph);
+	precond_free(S->P);
+	krylov_free(S->K);
+	for (void *p : S->owned) cudaFree(p);
+	delete S;
+}
+
+fv_status fv_solver_solve(fv_solver *S, double *u, const int *member_mask, fv_solve_stats *stats)
+{
+	if (!S || !u) { set_error("null argument"); return FV_ERR_INVALID; }
+	fv_disc_impl *D = S->D;
+	const int B = D->batch;
+	cudaStream_t s = D->stream;
+	cudaStream_t cs = nullptr;
+	cudaError_t e = cudaSuccess;
+	int *dmask = nullptr;
+	if (member_mask) {
+		e = cudaMalloc(&dmask, sizeof(int) * B);
+		if (!e) e = cudaMemcpy(dmask, member_mask, sizeof(int) * B, cudaMemcpyHostToDevice);
+	}
+	if (!e) {
+		k_init<<<(B + 31) / 32, 32, 0, s>>>(B, S->S, dmask);
+		count_launches(1);
+		e = cudaGetLastError();
+	}
+	S->mfop.u = u;
+	// graph of one step, specialised to this state pointer
+	const bool graph = S->cfg.use_graph != 0;
+	if (!e && graph) {
+		if (S->exec) { cudaGraphExecDestroy(S->exec); S->exec = nullptr; }
+		if (S->graph) { cudaGraphDestroy(S->graph); S->graph = nullptr; }
+		e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+		if (!e) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+		int nk = 0;
+		if (!e) {
+			cudaError_t e1 = solver_step(S, u, cs, &nk);
+			cudaError_t e2 = cudaStreamEndCapture(cs, &S->graph);
+			e = e1 ? e1 : e2;
+		}
+		if (!e) e = cudaGraphInstantiate(&S->exec, S->graph, 0);
+		S->kernels_per_step = nk;
+	}
+	std::vector<int> act(B), status(B, 0);
+	int steps_launched = 0;
+	const int maxit = S->cfg.max_timesteps;
+	while (!e && steps_launched < maxit) {
+		const int chunk = std::min(S->cfg.check_every, maxit - steps_launched);
+		for (int k = 0; k < chunk && !e; k++) {
+			if (graph) {
+				e = cudaGraphLaunch(S->exec, s);
+				count_launches(S->kernels_per_step);
+			} else {
+				int nk = 0;
+				e = solver_step(S, u, s, &nk);
+				count_launches(nk);
+				S->kernels_per_step = nk;
+			}
+		}
+		steps_launched += chunk;
+		if (!e) e = cudaMemcpyAsync(act.data(), S->S.active, sizeof(int) * B, cudaMemcpyDeviceToHost, s);
+		if (!e) e = cudaStreamSynchronize(s);
+		if (e) break;
+		bool any = false;
+		for (int b = 0; b < B; b++) any = any || act[b];
+		if (!any) break;
+	}
+	if (cs) cudaStreamDestroy(cs);
+	if (dmask) cudaFree(dmask);
+	if (e) return cuda_status(e, "steady solve");
+	// statistics
+	std::vector<double> res(B), res0(B), cfl(B);
+	std::vector<int> step(B), lin(B);
+	e = cudaMemcpy(res.data(), S->S.res, sizeof(double) * B, cudaMemcpyDeviceToHost);
+	if (!e) e = cudaMemcpy(res0.data(), S->S.res0, sizeof(double) * B, cudaMemcpyDeviceToHost);
+	if (!e) e = cudaMemcpy(cfl.data(), S->S.cfl, sizeof(double) * B, cudaMemcpyDeviceToHost);
+	if (!e) e = cudaMemcpy(step.data(), S->S.step, sizeof(int) * B, cudaMemcpyDeviceToHost);
+	if (!e) e = cudaMemcpy(lin.data(), S->S.linits, sizeof(int) * B, cudaMemcpyDeviceToHost);
+	if (!e) e = cudaMemcpy(status.data(), S->S.status, sizeof(int) * B, cudaMemcpyDeviceToHost);
+	if (e) return cuda_status(e, "solver statistics");
+	fv_status worst = FV_OK;
+	for (int b = 0; b < B; b++) {
+		int st = status[b];
+		if (st == ST_RUNNING) st = FV_ERR_TOLERANCE;
+		if (stats) {
+			stats[b].steps = step[b];
+			stats[b].lin_iters = lin[b];
+			stats[b].status = st == ST_PRECOND ? FV_ERR_NUMERICAL : st;
+			stats[b].res0 = res0[b];
+			stats[b].res = res[b];
+			stats[b].cfl = cfl[b];
+		}
+		if (st == ST_NUMERICAL || st == ST_PRECOND) worst = FV_ERR_NUMERICAL;
+		else if (st == FV_ERR_TOLERANCE && worst == FV_OK) worst = FV_ERR_TOLERANCE;
+	}
+	if (worst == FV_ERR_NUMERICAL) set_error("Steady backward Euler diverged - residual is Nan or inf!");
+	else if (worst == FV_ERR_TOLERANCE) set_error("Steady backward Euler did not converge to specified tolerance!");
+	return worst;
+}
+
+fv_status fv_solver_solve_host(fv_solver *S, double *h_u, const int *member_mask, fv_solve_stats *stats)
+{
+	if (!S || !h_u) { set_error("null argument"); return FV_ERR_INVALID; }
+	const size_t bytes = sizeof(double) * 4 * (size_t)S->D->d.nelem * S->D->batch;
+	double *d_u = nullptr;
+	cudaError_t e = cudaMalloc(&d_u, bytes);
+	if (!e) e = cudaMemcpyAsync(d_u, h_u, bytes, cudaMemcpyHostToDevice, S->D->stream);
+	if (e) { if (d_u) cudaFree(d_u); return cuda_status(e, "state upload"); }
+	fv_status st = fv_solver_solve(S, d_u, member_mask, stats);
+	e = cudaMemcpyAsync(h_u, d_u, bytes, cudaMemcpyDeviceToHost, S->D->stream);
+	if (!e) e = cudaStreamSynchronize(S->D->stream);
+	cudaFree(d_u);
+	if (e) return cuda_status(e, "state download");
+	return st;
+}
+
+fv_status fv_solver_history(const fv_solver *S, int member, int maxn, double *res, double *cfl, int *linits, int *n)
+{
+	if (!S || !n || member < 0 || member >= S->D->batch) { set_error("invalid argument"); return FV_ERR_INVALID; }
+	const int B = S->D->batch;
+	int step = 0;
+	cudaError_t e = cudaMemcpy(&step, S->S.step + member, sizeof(int), cudaMemcpyDeviceToHost);
+	if (e) return cuda_status(e, "history");
+	const int m = std::min(step, maxn);
+	std::vector<double> h(3 * (size_t)S->cfg.max_timesteps * B);
+	e = cudaMemcpy(h.data(), S->S.hist, sizeof(double) * h.size(), cudaMemcpyDeviceToHost);
+	if (e) return cuda_status(e, "history");
+	for (int k = 0; k < m; k++) {
+		const double *x = &h[((size_t)k * B + member) * 3];
+		if (res) res[k] = x[0];
+		if (cfl) cfl[k] = x[1];
+		if (linits) linits[k] = (int)x[2];
+	}
+	*n = m;
+	return FV_OK;
+}
+
+long long fv_solver_kernels_per_step(const fv_solver *S) { return S ? S->kernels_per_step : 0; }
+
+}  // extern "C"

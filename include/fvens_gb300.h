@@ -163,6 +163,66 @@ fv_status fv_matrix_add_diagonal(fv_disc *d, fv_matrix *A, const double *d_diag)
 fv_status fv_matrix_to_host(fv_disc *d, const fv_matrix *A, int member, int *nnzb, int *rowptr, int *col,
                             double *val);
 
+/* ---- preconditioners and Krylov solve (PETSc PC / KSP equivalents) ---- */
+typedef struct fv_precond fv_precond;
+/* type: FV_PC_*; the factor has the matrix's precision.  SGS and ILU(0)
+ * eliminate in the mesh's colour order (fv_precond_order). */
+fv_status fv_precond_create(fv_disc *d, fv_matrix *A, int type, fv_precond **out);
+void fv_precond_destroy(fv_precond *p);
+/* factorises / inverts from the matrix's current values; FV_ERR_NUMERICAL on a
+ * singular diagonal block.  Synchronises. */
+fv_status fv_precond_setup(fv_precond *p);
+/* d_z = M^{-1} d_r (all conditions of the batch) */
+fv_status fv_precond_apply(fv_precond *p, const double *d_r, double *d_z);
+/* elimination order: cell at each position (nelem ints) */
+fv_status fv_precond_order(const fv_precond *p, int *order);
+/* d_y = A d_x */
+fv_status fv_matvec(fv_disc *d, fv_matrix *A, const double *d_x, double *d_y);
+/* FGMRES(restart) on A x = b with the preconditioner's matrix, x0 = 0, stops
+ * when ||b - A x|| <= rtol ||b|| or after maxit iterations (maxit <= restart);
+ * h_iters[batch] receives the iteration counts.  Synchronises. */
+fv_status fv_ksp_solve(fv_precond *p, const double *d_b, double *d_x, int restart, int maxit, double rtol,
+                       int *h_iters);
+
+/* ---- steady implicit solver: SteadyBackwardEulerSolver (aodesolver.hpp, aodesolver.cpp:363-638) ---- */
+typedef struct fv_solver fv_solver;
+typedef struct {
+	double cfl_min, cfl_max;   /* pseudotime.main.cfl_min / cfl_max */
+	double tolerance;          /* pseudotime.main.tolerance */
+	int max_timesteps;         /* pseudotime.main.max_timesteps */
+	int abs_tolerance;         /* 1: ||R|| <= tolerance; 0: relative to step 0 (the reference) */
+	int pc_type;               /* FV_PC_* */
+	int ksp_restart, ksp_maxit;
+	double ksp_rtol;
+	int matrix_free;           /* -matrix_free_jacobian */
+	double mf_eps;             /* -matrix_free_difference_step */
+	int nl_update;             /* 0 full, 1 robust_flow (FlowSimpleUpdate) */
+	double min_relax;          /* min_nonlinear_relaxation_factor */
+	int precision;             /* stored Jacobian and preconditioner: 4 FP32, 8 FP64 */
+	int check_every;           /* steps between host polls of the convergence flags */
+	int use_graph;             /* replay each step as a captured CUDA graph */
+} fv_solver_cfg;
+typedef struct {
+	int steps, lin_iters, status; /* status: FV_OK, FV_ERR_NUMERICAL, FV_ERR_TOLERANCE */
+	double res0, res, cfl;        /* area-weighted energy-residual L2 norm at step 0 / last step; last CFL */
+} fv_solve_stats;
+
+void fv_solver_cfg_default(fv_solver_cfg *cfg);
+fv_status fv_solver_create(fv_disc *d, const fv_solver_cfg *cfg, fv_solver **out);
+void fv_solver_destroy(fv_solver *s);
+/* Solves every condition of the batch in place (d_u device state); member_mask
+ * (host, batch ints, NULL = all) selects conditions; stats[batch] per member.
+ * Returns FV_ERR_NUMERICAL if any member diverged, else FV_ERR_TOLERANCE if any
+ * member hit max_timesteps, else FV_OK.  Synchronises. */
+fv_status fv_solver_solve(fv_solver *s, double *d_u, const int *member_mask, fv_solve_stats *stats);
+/* The same with a host state: copies in, solves, copies out. */
+fv_status fv_solver_solve_host(fv_solver *s, double *h_u, const int *member_mask, fv_solve_stats *stats);
+/* convergence history of one member (aoutput.cpp:617-640 columns): residual
+ * norm, CFL and linear iterations per step; *n = steps written */
+fv_status fv_solver_history(const fv_solver *s, int member, int maxn, double *res, double *cfl, int *linits, int *n);
+/* kernels launched by one pseudo-time step (all members) */
+long long fv_solver_kernels_per_step(const fv_solver *s);
+
 /* ---- pointwise device evaluations (for validation against the reference) ---- */
 /* n states: d_ul, d_ur n x 4, d_n n x 2 -> d_f n x 4 (condition 0's physics) */
 fv_status fv_pointwise_flux(fv_disc *d, int kind, int n, const double *d_ul, const double *d_ur, const double *d_nrm,
