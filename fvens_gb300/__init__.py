@@ -74,6 +74,9 @@ def lib():
         L.fv_mesh_destroy.restype = None
         L.fv_disc_destroy.restype = None
         L.fv_matrix_destroy.restype = None
+        L.fv_precond_destroy.restype = None
+        L.fv_solver_destroy.restype = None
+        L.fv_solver_cfg_default.restype = None
         _lib = L
     return _lib
 
@@ -261,3 +264,123 @@ class BlockMatrix:
 
 def kernel_launch_count():
     return int(lib().fv_kernel_launch_count())
+
+
+class Preconditioner:
+    """PETSc PC equivalent on a BlockMatrix: 'jacobi', 'sgs' or 'ilu0'."""
+
+    def __init__(self, disc, matrix, kind="ilu0", ordering=1, part_size=128):
+        self.disc, self.matrix = disc, matrix
+        h = ctypes.c_void_p()
+        check(lib().fv_precond_create(disc._h, matrix._h, PC[kind], int(ordering), int(part_size), ctypes.byref(h)))
+        self._h = h
+
+    def setup(self):
+        check(lib().fv_precond_setup(self._h))
+
+    def apply(self, r, z):
+        check(lib().fv_precond_apply(self._h, _vp(dptr(r)), _vp(dptr(z))))
+
+    def order(self):
+        o = np.zeros(self.disc.nelem, np.int32)
+        check(lib().fv_precond_order(self._h, _hp(o, ctypes.c_int)))
+        return o
+
+    def ksp_solve(self, b, x, restart=30, maxit=30, rtol=0.1):
+        its = np.zeros(self.disc.batch, np.int32)
+        check(lib().fv_ksp_solve(self._h, _vp(dptr(b)), _vp(dptr(x)), int(restart), int(maxit), ctypes.c_double(rtol),
+                                 _hp(its, ctypes.c_int)))
+        return its
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fv_precond_destroy(self._h)
+            self._h = None
+
+
+def matvec(disc, matrix, x, y):
+    check(lib().fv_matvec(disc._h, matrix._h, _vp(dptr(x)), _vp(dptr(y))))
+
+
+class fv_solver_cfg(ctypes.Structure):
+    _fields_ = [("cfl_min", ctypes.c_double), ("cfl_max", ctypes.c_double), ("tolerance", ctypes.c_double),
+                ("max_timesteps", ctypes.c_int), ("abs_tolerance", ctypes.c_int), ("pc_type", ctypes.c_int),
+                ("ksp_restart", ctypes.c_int), ("ksp_maxit", ctypes.c_int), ("ksp_rtol", ctypes.c_double),
+                ("matrix_free", ctypes.c_int), ("mf_eps", ctypes.c_double), ("nl_update", ctypes.c_int),
+                ("min_relax", ctypes.c_double), ("precision", ctypes.c_int), ("check_every", ctypes.c_int),
+                ("use_graph", ctypes.c_int), ("pc_ordering", ctypes.c_int), ("pc_part_size", ctypes.c_int)]
+
+
+class fv_solve_stats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("lin_iters", ctypes.c_int), ("status", ctypes.c_int),
+                ("res0", ctypes.c_double), ("res", ctypes.c_double), ("cfl", ctypes.c_double)]
+
+
+def solver_cfg(**kw):
+    c = fv_solver_cfg()
+    lib().fv_solver_cfg_default(ctypes.byref(c))
+    names = {f[0] for f in fv_solver_cfg._fields_}
+    for k, v in kw.items():
+        if k == "pc":
+            c.pc_type = PC[v]
+        elif k == "nl_update" and isinstance(v, str):
+            c.nl_update = 0 if v == "full" else 1
+        elif k in names:
+            setattr(c, k, v)
+        else:
+            raise KeyError(k)
+    return c
+
+
+class SteadyBackwardEulerSolver:
+    """Implicit pseudo-time steady solver (reference SteadyBackwardEulerSolver)."""
+
+    def __init__(self, disc, cfg=None, **kw):
+        self.disc = disc
+        self.cfg = cfg if cfg is not None else solver_cfg(**kw)
+        h = ctypes.c_void_p()
+        check(lib().fv_solver_create(disc._h, ctypes.byref(self.cfg), ctypes.byref(h)))
+        self._h = h
+
+    def _stats(self, st):
+        return [dict(steps=s.steps, lin_iters=s.lin_iters, status=s.status, res0=s.res0, res=s.res, cfl=s.cfl)
+                for s in st]
+
+    def solve(self, u, member_mask=None, raise_on_error=True):
+        """Solves in place; u is a device array (batch x nelem x 4)."""
+        st = (fv_solve_stats * self.disc.batch)()
+        mask = None if member_mask is None else np.ascontiguousarray(member_mask, np.int32)
+        rc = lib().fv_solver_solve(self._h, _vp(dptr(u)), _hp(mask, ctypes.c_int) if mask is not None else None, st)
+        if raise_on_error:
+            check(rc)
+        return rc, self._stats(st)
+
+    def solve_host(self, u, member_mask=None, raise_on_error=True):
+        """Solves a host numpy state in place (copies in and out)."""
+        assert u.dtype == np.float64 and u.flags.c_contiguous
+        st = (fv_solve_stats * self.disc.batch)()
+        mask = None if member_mask is None else np.ascontiguousarray(member_mask, np.int32)
+        rc = lib().fv_solver_solve_host(self._h, _hp(u, ctypes.c_double),
+                                        _hp(mask, ctypes.c_int) if mask is not None else None, st)
+        if raise_on_error:
+            check(rc)
+        return rc, self._stats(st)
+
+    def history(self, member=0):
+        n = ctypes.c_int()
+        mx = self.cfg.max_timesteps
+        res = np.zeros(mx); cfl = np.zeros(mx); lin = np.zeros(mx, np.int32)
+        check(lib().fv_solver_history(self._h, int(member), mx, _hp(res, ctypes.c_double), _hp(cfl, ctypes.c_double),
+                                      _hp(lin, ctypes.c_int), ctypes.byref(n)))
+        k = n.value
+        return res[:k], cfl[:k], lin[:k]
+
+    def kernels_per_step(self):
+        L = lib()
+        L.fv_solver_kernels_per_step.restype = ctypes.c_longlong
+        return int(L.fv_solver_kernels_per_step(self._h))
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.fv_solver_destroy(self._h)
+            self._h = None

@@ -118,16 +118,14 @@ __global__ void __launch_bounds__(BS) k_diag_setup(int nelem, const RA *__restri
 	}
 }
 
-/* block ILU(0) of the rows of one colour (IKJ, no fill, colour elimination order) */
+/* block ILU(0) of the row at elimination position p (IKJ, no fill): every
+ * lower neighbour's row must already be final */
 template <class R, class RA>
-__global__ void __launch_bounds__(BS) k_ilu_colour(int nelem, int p0, int p1, const RA *__restrict__ A,
-                                                   const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
-                                                   const int4 *__restrict__ pnbrpos, R *__restrict__ F,
-                                                   R *__restrict__ Dinv, int *err, const int *active)
+__device__ __forceinline__ void ilu_row(int nelem, int p, int b, const RA *__restrict__ A,
+                                        const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
+                                        const int4 *__restrict__ pnbrpos, R *__restrict__ F, R *__restrict__ Dinv,
+                                        int *err)
 {
-	const int b = blockIdx.y;
-	const int p = p0 + blockIdx.x * BS + threadIdx.x;
-	if (p >= p1 || member_off(active, b)) return;
 	const size_t N = nelem;
 	const int i = pos_cell[p];
 	const RA *Ab = A + (size_t)b * 5 * N * 16;
@@ -180,17 +178,46 @@ __global__ void __launch_bounds__(BS) k_ilu_colour(int nelem, int p0, int p1, co
 	for (int s = 0; s < 5; s++) store_blk(Fb + ((size_t)s * N + p) * 16, row[s]);
 }
 
-/* forward sweep of one colour: y_p = r_i - sum_{lower} L y  (ILU) or
- * Dinv (r_i - sum_{lower} A y) (SGS) */
-template <class R>
-__global__ void __launch_bounds__(BS) k_fwd(int nelem, int p0, int p1, int sgs, const double *__restrict__ r,
-                                            const int *__restrict__ pos_cell, const int4 *__restrict__ pnbrpos,
-                                            const R *__restrict__ F, const R *__restrict__ Dinv, R *__restrict__ y,
-                                            const int *active)
+/* rows of one point colour (no dependencies inside the launch) */
+template <class R, class RA>
+__global__ void __launch_bounds__(BS) k_ilu_colour(int nelem, int p0, int p1, const RA *__restrict__ A,
+                                                   const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
+                                                   const int4 *__restrict__ pnbrpos, R *__restrict__ F,
+                                                   R *__restrict__ Dinv, int *err, const int *active)
 {
 	const int b = blockIdx.y;
 	const int p = p0 + blockIdx.x * BS + threadIdx.x;
 	if (p >= p1 || member_off(active, b)) return;
+	ilu_row<R, RA>(nelem, p, b, A, pos_cell, pnbr, pnbrpos, F, Dinv, err);
+}
+
+/* parts of one block colour: one CTA per part, levels separated by barriers */
+template <class R, class RA>
+__global__ void __launch_bounds__(BS) k_ilu_parts(int nelem, int part0, const int *__restrict__ part_ptr,
+                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
+                                                  const RA *__restrict__ A, const int *__restrict__ pos_cell,
+                                                  const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
+                                                  R *__restrict__ F, R *__restrict__ Dinv, int *err, const int *active)
+{
+	const int b = blockIdx.y;
+	if (member_off(active, b)) return;
+	const int part = part0 + blockIdx.x;
+	const int pend = part_ptr[part + 1];
+	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+	for (int l = l0; l < l1; l++) {
+		const int e = l + 1 < l1 ? lev_pos[l + 1] : pend;
+		for (int p = lev_pos[l] + threadIdx.x; p < e; p += BS) ilu_row<R, RA>(nelem, p, b, A, pos_cell, pnbr, pnbrpos, F, Dinv, err);
+		__syncthreads();
+	}
+}
+
+/* forward sweep of one colour: y_p = r_i - sum_{lower} L y  (ILU) or
+ * Dinv (r_i - sum_{lower} A y) (SGS) */
+template <class R>
+__device__ __forceinline__ void fwd_row(int nelem, int p, int b, int sgs, const double *__restrict__ r,
+                                        const int *__restrict__ pos_cell, const int4 *__restrict__ pnbrpos,
+                                        const R *__restrict__ F, const R *__restrict__ Dinv, R *__restrict__ y)
+{
 	const size_t N = nelem;
 	const int i = pos_cell[p];
 	const double4 *rb = reinterpret_cast<const double4 *>(r + (size_t)b * N * 4);
@@ -219,17 +246,45 @@ __global__ void __launch_bounds__(BS) k_fwd(int nelem, int p0, int p1, int sgs, 
 	}
 }
 
-/* backward sweep of one colour: z_i = Dinv (y_p - sum_{upper} U z) (ILU) or
- * y_p - Dinv sum_{upper} A z (SGS) */
 template <class R>
-__global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, const int *__restrict__ pos_cell,
-                                            const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
-                                            const R *__restrict__ F, const R *__restrict__ Dinv, const R *__restrict__ y,
-                                            double *__restrict__ z, const int *active)
+__global__ void __launch_bounds__(BS) k_fwd(int nelem, int p0, int p1, int sgs, const double *__restrict__ r,
+                                            const int *__restrict__ pos_cell, const int4 *__restrict__ pnbrpos,
+                                            const R *__restrict__ F, const R *__restrict__ Dinv, R *__restrict__ y,
+                                            const int *active)
 {
 	const int b = blockIdx.y;
 	const int p = p0 + blockIdx.x * BS + threadIdx.x;
 	if (p >= p1 || member_off(active, b)) return;
+	fwd_row<R>(nelem, p, b, sgs, r, pos_cell, pnbrpos, F, Dinv, y);
+}
+
+template <class R>
+__global__ void __launch_bounds__(BS) k_fwd_parts(int nelem, int part0, const int *__restrict__ part_ptr,
+                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
+                                                  int sgs, const double *__restrict__ r, const int *__restrict__ pos_cell,
+                                                  const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
+                                                  const R *__restrict__ Dinv, R *__restrict__ y, const int *active)
+{
+	const int b = blockIdx.y;
+	if (member_off(active, b)) return;
+	const int part = part0 + blockIdx.x;
+	const int pend = part_ptr[part + 1];
+	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+	for (int l = l0; l < l1; l++) {
+		const int e = l + 1 < l1 ? lev_pos[l + 1] : pend;
+		for (int p = lev_pos[l] + threadIdx.x; p < e; p += BS) fwd_row<R>(nelem, p, b, sgs, r, pos_cell, pnbrpos, F, Dinv, y);
+		__syncthreads();
+	}
+}
+
+/* backward sweep of one colour: z_i = Dinv (y_p - sum_{upper} U z) (ILU) or
+ * y_p - Dinv sum_{upper} A z (SGS) */
+template <class R>
+__device__ __forceinline__ void bwd_row(int nelem, int p, int b, int sgs, const int *__restrict__ pos_cell,
+                                        const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
+                                        const R *__restrict__ F, const R *__restrict__ Dinv, const R *__restrict__ y,
+                                        double *__restrict__ z)
+{
 	const size_t N = nelem;
 	const int i = pos_cell[p];
 	const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
@@ -259,6 +314,40 @@ __global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, 
 		mv(d, v, out);
 	}
 	reinterpret_cast<double4 *>(zb)[i] = make_double4(double(out[0]), double(out[1]), double(out[2]), double(out[3]));
+}
+
+template <class R>
+__global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, const int *__restrict__ pos_cell,
+                                            const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
+                                            const R *__restrict__ F, const R *__restrict__ Dinv, const R *__restrict__ y,
+                                            double *__restrict__ z, const int *active)
+{
+	const int b = blockIdx.y;
+	const int p = p0 + blockIdx.x * BS + threadIdx.x;
+	if (p >= p1 || member_off(active, b)) return;
+	bwd_row<R>(nelem, p, b, sgs, pos_cell, pnbr, pnbrpos, F, Dinv, y, z);
+}
+
+/* backward sweep of the parts of one block colour: levels in reverse (a cell's
+ * upper neighbours inside its part sit on higher forward levels) */
+template <class R>
+__global__ void __launch_bounds__(BS) k_bwd_parts(int nelem, int part0, const int *__restrict__ part_ptr,
+                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
+                                                  int sgs, const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
+                                                  const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
+                                                  const R *__restrict__ Dinv, const R *__restrict__ y,
+                                                  double *__restrict__ z, const int *active)
+{
+	const int b = blockIdx.y;
+	if (member_off(active, b)) return;
+	const int part = part0 + blockIdx.x;
+	const int pend = part_ptr[part + 1];
+	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+	for (int l = l1 - 1; l >= l0; l--) {
+		const int e = l + 1 < l1 ? lev_pos[l + 1] : pend;
+		for (int p = lev_pos[l] + threadIdx.x; p < e; p += BS) bwd_row<R>(nelem, p, b, sgs, pos_cell, pnbr, pnbrpos, F, Dinv, y, z);
+		__syncthreads();
+	}
 }
 
 template <class R>
@@ -489,6 +578,14 @@ cudaError_t precond_setup_t(Precond &P, int *err, const int *active, cudaStream_
 		if (P.type == PC_JACOBI || P.type == PC_SGS) {
 			k_diag_setup<R><<<dim3((N + BS - 1) / BS, B), BS, 0, s>>>(N, A, P.pos_cell, F, D, P.type == PC_SGS, err, active);
 			(*nk)++;
+		} else if (P.type == PC_ILU0 && P.ordering == 1) {
+			for (int c = 0; c < P.ncolors; c++) {
+				const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
+				if (q1 <= q0) continue;
+				k_ilu_parts<R><<<dim3(q1 - q0, B), BS, 0, s>>>(N, q0, P.part_ptr, P.lev_ptr, P.lev_pos, A, P.pos_cell,
+				                                               P.pnbr, P.pnbrpos, F, D, err, active);
+				(*nk)++;
+			}
 		} else if (P.type == PC_ILU0) {
 			for (int c = 0; c < P.ncolors; c++) {
 				const int p0 = P.cptr[c], p1 = P.cptr[c + 1];
@@ -517,6 +614,22 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 	} else if (P.type == PC_JACOBI) {
 		k_jacobi_apply<R><<<dim3((N + BS - 1) / BS, B), BS, 0, s>>>(N, r, P.cell_pos, D, z, active);
 		(*nk)++;
+	} else if (P.ordering == 1) {
+		const int sgs = P.type == PC_SGS;
+		for (int c = 0; c < P.ncolors; c++) {
+			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
+			if (q1 <= q0) continue;
+			k_fwd_parts<R><<<dim3(q1 - q0, B), BS, 0, s>>>(N, q0, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell,
+			                                               P.pnbrpos, F, D, y, active);
+			(*nk)++;
+		}
+		for (int c = P.ncolors - 1; c >= 0; c--) {
+			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
+			if (q1 <= q0) continue;
+			k_bwd_parts<R><<<dim3(q1 - q0, B), BS, 0, s>>>(N, q0, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell,
+			                                               P.pnbr, P.pnbrpos, F, D, y, z, active);
+			(*nk)++;
+		}
 	} else {
 		const int sgs = P.type == PC_SGS;
 		for (int c = 0; c < P.ncolors; c++) {
@@ -537,18 +650,35 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 
 }  // namespace
 
-cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec)
+cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec, int ordering, int part_size)
 {
 	P.type = type;
+	P.ordering = ordering;
+	P.part_size = part_size;
 	P.prec = prec;
 	P.batch = batch;
 	const HostMesh &h = m->h;
 	const int N = h.nelem;
 	P.nelem = N;
-	P.ncolors = h.ncolors;
-	P.cptr = h.color_ptr;
-	std::vector<int> pos_cell = h.color_cells, cell_pos(N);
+	std::vector<int> pos_cell, cell_pos(N);
+	std::vector<int> part_ptr, lev_ptr, lev_pos;
+	if (P.ordering == 1) {
+		const BlockOrder bo = block_colour_order(h, P.part_size);
+		P.ncolors = bo.ncolors;
+		P.cpart = bo.cpart_ptr;
+		pos_cell = bo.pos_cell;
+		part_ptr = bo.part_ptr;
+		lev_ptr = bo.lev_ptr;
+		lev_pos = bo.lev_pos;
+		P.nparts = bo.nparts;
+		P.max_width = bo.max_width;
+	} else {
+		P.ncolors = h.ncolors;
+		P.cptr = h.color_ptr;
+		pos_cell = h.color_cells;
+	}
 	for (int p = 0; p < N; p++) cell_pos[pos_cell[p]] = p;
+	P.order_h = pos_cell;
 	std::vector<int4> pn(N), pp(N);
 	for (int p = 0; p < N; p++) {
 		const int i = pos_cell[p];
@@ -571,6 +701,11 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 	up((void **)&P.cell_pos, cell_pos.data(), sizeof(int) * N);
 	up((void **)&P.pnbr, pn.data(), sizeof(int4) * N);
 	up((void **)&P.pnbrpos, pp.data(), sizeof(int4) * N);
+	if (P.ordering == 1) {
+		up((void **)&P.part_ptr, part_ptr.data(), sizeof(int) * part_ptr.size());
+		up((void **)&P.lev_ptr, lev_ptr.data(), sizeof(int) * lev_ptr.size());
+		up((void **)&P.lev_pos, lev_pos.data(), sizeof(int) * lev_pos.size());
+	}
 	const size_t w = prec;
 	if (!e && (type == PC_SGS || type == PC_ILU0)) e = cudaMalloc(&P.F, (size_t)batch * 5 * N * 16 * w);
 	if (!e) e = cudaMalloc(&P.Dinv, (size_t)batch * N * 16 * w);
@@ -580,11 +715,12 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 
 void precond_free(Precond &P)
 {
-	void *ps[] = {P.pos_cell, P.cell_pos, P.pnbr, P.pnbrpos, P.F, P.Dinv, P.y};
+	void *ps[] = {P.pos_cell, P.cell_pos, P.pnbr, P.pnbrpos, P.F, P.Dinv, P.y, P.part_ptr, P.lev_ptr, P.lev_pos};
 	for (void *p : ps)
 		if (p) cudaFree(p);
 	P.pos_cell = nullptr; P.cell_pos = nullptr; P.pnbr = nullptr; P.pnbrpos = nullptr;
 	P.F = nullptr; P.Dinv = nullptr; P.y = nullptr;
+	P.part_ptr = nullptr; P.lev_ptr = nullptr; P.lev_pos = nullptr;
 }
 
 cudaError_t precond_setup(Precond &P, int *err, const int *active, cudaStream_t s, int *nk)

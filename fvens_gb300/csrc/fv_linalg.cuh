@@ -4,10 +4,13 @@
 //
 // Replaces PETSc's -pc_type pbjacobi / sor / bjacobi+ilu on BAIJ(4) and
 // KSPFGMRES (external to the reference; called from aodesolver.cpp:483).
-// The elimination order of SGS and ILU(0) is the mesh's colour order (cells of
-// colour 0, then colour 1, ...): cells of one colour share no face, so each
-// colour is one fully parallel launch.  The factor is stored in colour order
-// so those launches read contiguous blocks.
+// The elimination order of SGS and ILU(0) is either the block-colour order
+// (default: compact parts of ~128 cells, parts coloured so that parts of one
+// colour share no face; one launch per colour, one CTA per part sweeping the
+// part's dependency levels with a barrier between levels) or the point-colour
+// order (cells of one colour share no face; one fully parallel launch per
+// colour).  The factor is stored in elimination order so each launch reads
+// contiguous blocks.
 #pragma once
 #include "fv_core.cuh"
 
@@ -18,7 +21,15 @@ struct Precond {
 	int type = PC_NONE;
 	int prec = 4;               // 4: FP32 factor, 8: FP64 factor
 	int nelem = 0, batch = 1, ncolors = 0;
-	std::vector<int> cptr;      // colour ranges in the colour-ordered position space
+	int ordering = 1;           // 0: point colours, 1: block colours (parts of ~part_size cells)
+	int part_size = 128;
+	int nparts = 0, max_width = 0;
+	std::vector<int> cptr;      // point colours: position range of each colour
+	std::vector<int> cpart;     // block colours: part range of each colour
+	int *part_ptr = nullptr;    // [nparts+1] position range of each part
+	int *lev_ptr = nullptr;     // [nparts+1] range of each part's levels in lev_pos
+	int *lev_pos = nullptr;     // level start positions
+	std::vector<int> order_h;   // host copy of the elimination order (position -> cell)
 	int *pos_cell = nullptr;    // [nelem] cell at colour-order position p
 	int *cell_pos = nullptr;    // [nelem] position of cell i
 	int4 *pnbr = nullptr;       // [nelem] neighbours (as cells) of the cell at position p, -1 none
@@ -29,7 +40,9 @@ struct Precond {
 	BlockMatrix *A = nullptr;   // source matrix (cell order)
 };
 
-cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec);
+/* ordering: 0 point colours, 1 block colours with parts of ~part_size cells */
+cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec, int ordering = 1,
+                          int part_size = 128);
 void precond_free(Precond &P);
 /* factorisation / diagonal inversion from P.A; err_flag (device int) is set
  * non-zero when a diagonal block is singular */

@@ -575,3 +575,108 @@ int read_gmsh2(const std::string &path, RawMesh &out, std::string *err)
 }
 
 }  // namespace fvg
+
+namespace fvg {
+
+namespace {
+void rcb_split(const std::vector<double> &cc, std::vector<int> &idx, size_t lo, size_t hi, size_t target,
+               std::vector<std::pair<size_t, size_t>> &parts)
+{
+	if (hi - lo <= target) {
+		parts.push_back({lo, hi});
+		return;
+	}
+	double mn[2] = {1e300, 1e300}, mx[2] = {-1e300, -1e300};
+	for (size_t k = lo; k < hi; k++)
+		for (int d = 0; d < 2; d++) {
+			mn[d] = std::min(mn[d], cc[2 * idx[k] + d]);
+			mx[d] = std::max(mx[d], cc[2 * idx[k] + d]);
+		}
+	const int d = (mx[0] - mn[0]) >= (mx[1] - mn[1]) ? 0 : 1;
+	std::stable_sort(idx.begin() + lo, idx.begin() + hi, [&](int a, int b) {
+		const double xa = cc[2 * a + d], xb = cc[2 * b + d];
+		return xa < xb || (xa == xb && a < b);
+	});
+	const size_t mid = lo + (hi - lo) / 2;
+	rcb_split(cc, idx, lo, mid, target, parts);
+	rcb_split(cc, idx, mid, hi, target, parts);
+}
+}  // namespace
+
+BlockOrder block_colour_order(const HostMesh &h, int part_size)
+{
+	BlockOrder o;
+	const int n = h.nelem;
+	std::vector<int> idx(n);
+	std::iota(idx.begin(), idx.end(), 0);
+	std::vector<std::pair<size_t, size_t>> ranges;
+	rcb_split(h.cc, idx, 0, n, std::max(part_size, 1), ranges);
+	const int np = (int)ranges.size();
+	std::vector<int> pid(n);
+	std::vector<std::vector<int>> cells(np);
+	for (int k = 0; k < np; k++) {
+		for (size_t q = ranges[k].first; q < ranges[k].second; q++) {
+			pid[idx[q]] = k;
+			cells[k].push_back(idx[q]);
+		}
+		std::sort(cells[k].begin(), cells[k].end());
+	}
+	// colour the part adjacency graph greedily
+	std::vector<std::vector<int>> padj(np);
+	for (int f = h.nbface; f < h.naface; f++) {
+		const int a = pid[h.face_l[f]], b = pid[h.face_r[f]];
+		if (a != b) { padj[a].push_back(b); padj[b].push_back(a); }
+	}
+	std::vector<int> pcol(np, -1);
+	int nc = 0;
+	for (int k = 0; k < np; k++) {
+		std::vector<char> used(64, 0);
+		for (int j : padj[k])
+			if (pcol[j] >= 0 && pcol[j] < 64) used[pcol[j]] = 1;
+		int c = 0;
+		while (used[c]) c++;
+		pcol[k] = c;
+		nc = std::max(nc, c + 1);
+	}
+	o.nparts = np;
+	o.ncolors = nc;
+	o.part_ptr.push_back(0);
+	o.cpart_ptr.assign(nc + 1, 0);
+	o.lev_ptr.push_back(0);
+	std::vector<int> level(n, 0);
+	for (int c = 0; c < nc; c++) {
+		for (int k = 0; k < np; k++) {
+			if (pcol[k] != c) continue;
+			// levels of the lower-triangular dependencies inside the part (cells in index order)
+			int maxl = 0;
+			for (int i : cells[k]) {
+				int l = 0;
+				for (int j = 0; j < h.nnode[i]; j++) {
+					const int nb = h.esuel[4 * i + j];
+					if (nb >= 0 && nb < i && pid[nb] == k) l = std::max(l, level[nb] + 1);
+				}
+				level[i] = l;
+				maxl = std::max(maxl, l);
+			}
+			std::vector<int> sorted = cells[k];
+			std::stable_sort(sorted.begin(), sorted.end(), [&](int a, int b) { return level[a] < level[b]; });
+			const int base = (int)o.pos_cell.size();
+			for (size_t q = 0; q < sorted.size(); q++) {
+				if (q == 0 || level[sorted[q]] != level[sorted[q - 1]]) o.lev_pos.push_back(base + (int)q);
+				o.pos_cell.push_back(sorted[q]);
+			}
+			// widest level
+			for (size_t q = 0, s = 0; q <= sorted.size(); q++)
+				if (q == sorted.size() || (q > 0 && level[sorted[q]] != level[sorted[q - 1]])) {
+					o.max_width = std::max(o.max_width, (int)(q - s));
+					s = q;
+				}
+			o.lev_ptr.push_back((int)o.lev_pos.size());
+			o.part_ptr.push_back((int)o.pos_cell.size());
+		}
+		o.cpart_ptr[c + 1] = (int)o.part_ptr.size() - 1;
+	}
+	return o;
+}
+
+}  // namespace fvg

@@ -52,6 +52,25 @@ struct HostMesh {
 int mesh_from_arrays(HostMesh &m, int npoin, const double *coords, int nelem, const int *nnode, const int *inpoel,
                      int nbface, const int *bface, const int *btag, int reorder, std::string *err);
 
+/* Block-colour elimination order for the SGS / ILU(0) preconditioners:
+ * cells are split into compact parts of about part_size cells by recursive
+ * coordinate bisection of the centroids, parts sharing a face get different
+ * colours, and the order is colour-major, then part-major, then inside a part
+ * by dependency level (ties by cell index).  Within a part the relative order
+ * of any two adjacent cells is their index order, so ILU(0) on this order
+ * equals ILU(0) on the cell order with the couplings between same-colour parts
+ * absent (there are none); the levels let one CTA sweep a part with a barrier
+ * between levels. */
+struct BlockOrder {
+	int nparts = 0, ncolors = 0, max_width = 0;
+	std::vector<int> pos_cell;   // elimination position -> cell
+	std::vector<int> part_ptr;   // part -> position range
+	std::vector<int> cpart_ptr;  // colour -> part range
+	std::vector<int> lev_ptr;    // part -> range in lev_pos
+	std::vector<int> lev_pos;    // level start positions (each part's levels in order)
+};
+BlockOrder block_colour_order(const HostMesh &h, int part_size);
+
 /* Reverse Cuthill-McKee ordering of the cell graph (own implementation:
  * George-Liu pseudo-peripheral start, neighbours visited by increasing degree). */
 std::vector<int> rcm_order(int n, const std::vector<int> &adj_ptr, const std::vector<int> &adj);

@@ -349,7 +349,7 @@ cudaError_t solver_step(fv_solver *S, double *u, cudaStream_t s, int *nk)
 
 extern "C" {
 
-fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, fv_precond **out)
+fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, int ordering, int part_size, fv_precond **out)
 {
 	if (!D || !M || !out || M->owner != D || type < FV_PC_NONE || type > FV_PC_ILU0) {
 		set_error("invalid argument");
@@ -358,7 +358,7 @@ fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, fv_precond **out
 	fv_precond *p = new fv_precond();
 	p->D = D;
 	p->M = M;
-	cudaError_t e = precond_alloc(p->P, D->mesh, D->batch, type, M->A.prec);
+	cudaError_t e = precond_alloc(p->P, D->mesh, D->batch, type, M->A.prec, ordering ? 1 : 0, part_size > 0 ? part_size : 128);
 	p->P.A = &M->A;
 	if (!e) e = cudaMalloc(&p->err, sizeof(int));
 	if (!e) e = cudaMemset(p->err, 0, sizeof(int));
@@ -410,9 +410,7 @@ fv_status fv_precond_apply(fv_precond *p, const double *r, double *z)
 fv_status fv_precond_order(const fv_precond *p, int *order)
 {
 	if (!p || !order) { set_error("null argument"); return FV_ERR_INVALID; }
-	const HostMesh &h = p->D->mesh->h;
-	if (p->P.type == FV_PC_SGS || p->P.type == FV_PC_ILU0) std::memcpy(order, h.color_cells.data(), sizeof(int) * h.nelem);
-	else for (int i = 0; i < h.nelem; i++) order[i] = i;
+	std::memcpy(order, p->P.order_h.data(), sizeof(int) * p->P.order_h.size());
 	return FV_OK;
 }
 
@@ -453,7 +451,7 @@ void fv_solver_cfg_default(fv_solver_cfg *c)
 	c->cfl_min = 10; c->cfl_max = 1000; c->tolerance = 1e-10; c->max_timesteps = 1000; c->abs_tolerance = 1;
 	c->pc_type = FV_PC_ILU0; c->ksp_restart = 30; c->ksp_maxit = 30; c->ksp_rtol = 0.1;
 	c->matrix_free = 0; c->mf_eps = 1e-7; c->nl_update = 0; c->min_relax = 0.2; c->precision = 4;
-	c->check_every = 4; c->use_graph = 1;
+	c->check_every = 4; c->use_graph = 1; c->pc_ordering = 1; c->pc_part_size = 128;
 }
 
 fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out)
@@ -480,7 +478,8 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	cudaError_t e = cudaSuccess;
 	if (!e) e = salloc(S, (char **)&S->A.val, S->A.nval() * cfg->precision);
 	if (!e) e = salloc(S, &S->A.bdiag, 16 * (size_t)B * std::max(D->d.nbface, 1));
-	if (!e) e = precond_alloc(S->P, D->mesh, B, cfg->pc_type, cfg->precision);
+	if (!e) e = precond_alloc(S->P, D->mesh, B, cfg->pc_type, cfg->precision, cfg->pc_ordering ? 1 : 0,
+	                          cfg->pc_part_size > 0 ? cfg->pc_part_size : 128);
 	S->P.A = &S->A;
 	if (!e) e = krylov_alloc(S->K, 4 * N, B, cfg->ksp_restart);
 	S->nblk = std::max(1, std::min(256, (N + RBS * 8 - 1) / (RBS * 8)));

@@ -166,8 +166,10 @@ fv_status fv_matrix_to_host(fv_disc *d, const fv_matrix *A, int member, int *nnz
 /* ---- preconditioners and Krylov solve (PETSc PC / KSP equivalents) ---- */
 typedef struct fv_precond fv_precond;
 /* type: FV_PC_*; the factor has the matrix's precision.  SGS and ILU(0)
- * eliminate in the mesh's colour order (fv_precond_order). */
-fv_status fv_precond_create(fv_disc *d, fv_matrix *A, int type, fv_precond **out);
+ * eliminate in a colour order (fv_precond_order): ordering 1 = block colours
+ * (compact parts of ~part_size cells, natural order inside a part; the
+ * default), 0 = point colours. */
+fv_status fv_precond_create(fv_disc *d, fv_matrix *A, int type, int ordering, int part_size, fv_precond **out);
 void fv_precond_destroy(fv_precond *p);
 /* factorises / inverts from the matrix's current values; FV_ERR_NUMERICAL on a
  * singular diagonal block.  Synchronises. */
@@ -201,6 +203,8 @@ typedef struct {
 	int precision;             /* stored Jacobian and preconditioner: 4 FP32, 8 FP64 */
 	int check_every;           /* steps between host polls of the convergence flags */
 	int use_graph;             /* replay each step as a captured CUDA graph */
+	int pc_ordering;           /* 1 block colours (default), 0 point colours */
+	int pc_part_size;          /* cells per part of the block-colour order (default 128) */
 } fv_solver_cfg;
 typedef struct {
 	int steps, lin_iters, status; /* status: FV_OK, FV_ERR_NUMERICAL, FV_ERR_TOLERANCE */

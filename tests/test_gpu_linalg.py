@@ -1,0 +1,89 @@
+"""GPU preconditioners, block SpMV and FGMRES against the oracle's
+restatement of PETSc's block ILU(0) / SOR(SGS) / point-block Jacobi and
+FGMRES, on the same matrix and the same elimination order."""
+import numpy as np
+import pytest
+
+import fvens_gb300 as fv
+from oracle import orc
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(cuda, prec, mesh=None):
+    """C1-like Jacobian at a perturbed state plus a pseudo-time diagonal
+    (as the solver builds it at CFL 50)."""
+    import torch
+    m = mesh or cases.channel(48, 16)
+    gd = fv.FlowFV(m, fv.physics_cfg(Minf=0.5), fv.numerics_cfg(flux="ROE"), cases.CHANNEL_BCS)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), Minf=0.5, flux="ROE", bcs=cases.CHANNEL_BCS)
+    u = cases.perturbed_state(od.freestream(), m.nelem)
+    ud = torch.tensor(u, device=cuda)
+    A = fv.BlockMatrix(gd, prec)
+    gd.assemble_jacobian(ud, A)
+    _, dt = od.residual(u)
+    diag = m.geometry()["area"] / (50.0 * dt)
+    A.add_diagonal(torch.tensor(diag, device=cuda))
+    rp, col, val = A.to_host()
+    return m, gd, A, rp, col, val
+
+
+@pytest.mark.parametrize("prec,tol", [(8, 1e-11), (4, 3e-5)])
+@pytest.mark.parametrize("kind", ["jacobi", "sgs", "ilu0"])
+@pytest.mark.parametrize("ordering", [1, 0])
+def test_precond_apply(cuda, prec, tol, kind, ordering):
+    import torch
+    m, gd, A, rp, col, val = _system(cuda, prec)
+    P = fv.Preconditioner(gd, A, kind, ordering=ordering, part_size=64)
+    P.setup()
+    rng = np.random.default_rng(5)
+    r = rng.normal(size=(m.nelem, 4))
+    z = torch.zeros((m.nelem, 4), dtype=torch.float64, device=cuda)
+    P.apply(torch.tensor(r, device=cuda), z)
+    zo = orc.precond_apply(rp, col, val, kind, r.ravel(), order=P.order()).reshape(-1, 4)
+    err = np.abs(z.cpu().numpy() - zo).max() / np.abs(zo).max()
+    assert err <= tol, f"{kind} prec {prec} ordering {ordering}: {err:.3e}"
+
+
+def test_block_order_is_valid(cuda):
+    m, gd, A, rp, col, val = _system(cuda, 8, mesh=cases.channel(96, 32))
+    P = fv.Preconditioner(gd, A, "ilu0", ordering=1, part_size=128)
+    order = P.order()
+    assert np.array_equal(np.sort(order), np.arange(m.nelem))
+
+
+def test_spmv(cuda):
+    import torch
+    m, gd, A, rp, col, val = _system(cuda, 8)
+    x = np.random.default_rng(2).normal(size=(m.nelem, 4))
+    y = torch.zeros((m.nelem, 4), dtype=torch.float64, device=cuda)
+    fv.matvec(gd, A, torch.tensor(x, device=cuda), y)
+    yo = np.zeros_like(x)
+    for i in range(m.nelem):
+        for k in range(rp[i], rp[i + 1]):
+            yo[i] += val[k].reshape(4, 4) @ x[col[k]]
+    assert np.abs(y.cpu().numpy() - yo).max() <= 1e-12 * np.abs(yo).max()
+
+
+@pytest.mark.parametrize("kind", ["ilu0", "sgs"])
+def test_fgmres_matches_oracle(cuda, kind):
+    """FP64 matrix and factor: same Krylov iterates as the oracle's FGMRES."""
+    import torch
+    m, gd, A, rp, col, val = _system(cuda, 8)
+    P = fv.Preconditioner(gd, A, kind, ordering=1, part_size=64)
+    P.setup()
+    b = np.random.default_rng(9).normal(size=(m.nelem, 4))
+    x = torch.zeros_like(torch.tensor(b, device=cuda))
+    its = P.ksp_solve(torch.tensor(b, device=cuda), x, restart=30, maxit=30, rtol=1e-6)
+    xo, itso, rno = orc.fgmres(rp, col, val, kind, b.ravel(), restart=30, maxit=30, rtol=1e-6, order=P.order())
+    assert its[0] == itso
+    err = np.abs(x.cpu().numpy().ravel() - xo).max() / np.abs(xo).max()
+    assert err <= 1e-8, err
+    # the iterate really reduces the residual by rtol
+    res = b.ravel().copy()
+    xx = x.cpu().numpy()
+    for i in range(m.nelem):
+        for k in range(rp[i], rp[i + 1]):
+            res[4 * i:4 * i + 4] -= val[k].reshape(4, 4) @ xx[col[k]]
+    assert np.linalg.norm(res) <= 1.01e-6 * np.linalg.norm(b)

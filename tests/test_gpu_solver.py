@@ -1,0 +1,106 @@
+"""Steady implicit solves on the GPU against the oracle's restatement of
+SteadyBackwardEulerSolver::solve: converged states, step counts, failure
+reporting."""
+import numpy as np
+import pytest
+
+import fvens_gb300 as fv
+from oracle import orc
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(nx=48, ny=16, **phys):
+    m = cases.channel(nx, ny)
+    pk = dict(Minf=0.5, **phys)
+    gd = fv.FlowFV(m, fv.physics_cfg(**pk), fv.numerics_cfg(flux="ROE"), cases.CHANNEL_BCS)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), **pk, flux="ROE", bcs=cases.CHANNEL_BCS)
+    return m, gd, od
+
+
+@pytest.mark.parametrize("prec", [8, 4])
+def test_c1_like_solve_matches_oracle(cuda, prec):
+    import torch
+    m, gd, od = _setup()
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200,
+                                     pc="ilu0", precision=prec)
+    ud = torch.tensor(u0, device=cuda)
+    rc, st = S.solve(ud)
+    P = fv.Preconditioner(gd, fv.BlockMatrix(gd, prec), "ilu0")
+    uo, sto = od.steady_solve(u0, cflmin=10, cflmax=1000, tol=1e-10, maxiter=200, pc="ilu0", order=P.order())
+    assert st[0]["status"] == 0 and sto["status"] == 0
+    assert st[0]["res"] <= 1e-10
+    # converged fields agree (both at ||R|| < 1e-10)
+    ug = ud.cpu().numpy()
+    assert np.abs(ug - uo).max() / np.abs(uo).max() <= 1e-8
+    if prec == 8:
+        assert abs(st[0]["steps"] - sto["steps"]) <= 2
+    res, cfl, lin = S.history()
+    assert len(res) == st[0]["steps"] and cfl[0] == 10.0
+
+
+def test_matrix_free_solve(cuda):
+    import torch
+    m, gd, od = _setup()
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200,
+                                     pc="ilu0", precision=4, matrix_free=1)
+    ud = torch.tensor(u0, device=cuda)
+    rc, st = S.solve(ud)
+    assert st[0]["status"] == 0
+    r = torch.zeros_like(ud)
+    gd.compute_residual(ud, r)
+    a = m.geometry()["area"]
+    assert np.sqrt((r.cpu().numpy()[:, 3] ** 2 * a).sum()) < 1e-9
+
+
+def test_batched_solve_matches_single(cuda):
+    import torch
+    m = cases.channel(48, 16)
+    plist = [dict(Minf=0.5), dict(Minf=0.4, aoa_deg=1.0), dict(Minf=0.55, aoa_deg=-0.5)]
+    gd = fv.FlowFV(m, [fv.physics_cfg(**p) for p in plist], fv.numerics_cfg(flux="ROE"), cases.CHANNEL_BCS)
+    u0 = np.concatenate([np.tile(u, (m.nelem, 1)) for u in gd.freestream()])
+    ud = torch.tensor(u0, device=cuda)
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200, precision=4)
+    rc, st = S.solve(ud)
+    assert all(s["status"] == 0 for s in st)
+    for k, p in enumerate(plist):
+        g1 = fv.FlowFV(m, fv.physics_cfg(**p), fv.numerics_cfg(flux="ROE"), cases.CHANNEL_BCS)
+        u1 = torch.tensor(np.tile(g1.freestream()[0], (m.nelem, 1)), device=cuda)
+        fv.SteadyBackwardEulerSolver(g1, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200,
+                                     precision=4).solve(u1)
+        a = ud.cpu().numpy()[k * m.nelem:(k + 1) * m.nelem]
+        assert np.abs(a - u1.cpu().numpy()).max() / np.abs(a).max() <= 1e-8
+
+
+def test_divergence_reports_numerical_error(cuda):
+    """PseudotimeFlow_exception_nanorinf (tests/flowpseudotime.cpp): a state
+    that makes the residual non-finite ends the solve with
+    FV_ERR_NUMERICAL (the reference throws Numerical_error).  The fault is
+    injected on the host, in the initial state."""
+    import torch
+    m, gd, od = _setup()
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    u0[5, 3] = -1.0  # negative energy: negative pressure, sound speed NaN
+    S = fv.SteadyBackwardEulerSolver(gd, max_timesteps=20, precision=4)
+    rc, st = S.solve(torch.tensor(u0, device=cuda), raise_on_error=False)
+    assert rc == fv.FV_ERR_NUMERICAL and st[0]["status"] == fv.FV_ERR_NUMERICAL
+
+
+def test_max_steps_reports_tolerance_error(cuda):
+    import torch
+    m, gd, od = _setup()
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    S = fv.SteadyBackwardEulerSolver(gd, max_timesteps=3, precision=4)
+    rc, st = S.solve(torch.tensor(u0, device=cuda), raise_on_error=False)
+    assert rc == fv.FV_ERR_TOLERANCE and st[0]["steps"] == 3
+
+
+def test_host_buffer_solve(cuda):
+    m, gd, od = _setup()
+    u = np.ascontiguousarray(np.tile(od.freestream(), (m.nelem, 1)))
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200, precision=4)
+    rc, st = S.solve_host(u)
+    assert st[0]["status"] == 0 and np.all(np.isfinite(u))
