@@ -113,6 +113,9 @@ struct fv_disc_impl {
 cudaError_t residual_launch(fv_disc_impl *D, const double *u, double *r, int gettimesteps, double *dt,
                             cudaStream_t s);
 cudaError_t gradients_launch(fv_disc_impl *D, const double *u, double *grad, int conserved, cudaStream_t s);
+/* the face-flux launch alone (reads the prep/gradient/limiter results of the
+ * last residual evaluation of the same state) */
+cudaError_t face_launch(fv_disc_impl *D, const double *u, int gettimesteps, cudaStream_t s);
 
 /* Block-row matrix: 5 slots per cell (0 = diagonal, 1+j = neighbour across
  * local edge j); values [batch][slot][cell][16], FP32 or FP64. */

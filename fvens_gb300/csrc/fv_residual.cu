@@ -77,6 +77,22 @@ void launch_face(fv_disc_impl *Dh, const double *u, int getdt, dim3 grid, cudaSt
 
 }  // namespace
 
+cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cudaStream_t s)
+{
+	const DiscDev &D = Dh->d;
+	const dim3 gf((unsigned)((D.naface + BS - 1) / BS), (unsigned)Dh->batch);
+	switch (D.flux) {
+	case FLUX_LLF: launch_face<FLUX_LLF>(Dh, u, gettimesteps, gf, s); break;
+	case FLUX_VANLEER: launch_face<FLUX_VANLEER>(Dh, u, gettimesteps, gf, s); break;
+	case FLUX_AUSM: launch_face<FLUX_AUSM>(Dh, u, gettimesteps, gf, s); break;
+	case FLUX_AUSMPLUS: launch_face<FLUX_AUSMPLUS>(Dh, u, gettimesteps, gf, s); break;
+	case FLUX_ROE: launch_face<FLUX_ROE>(Dh, u, gettimesteps, gf, s); break;
+	case FLUX_HLL: launch_face<FLUX_HLL>(Dh, u, gettimesteps, gf, s); break;
+	default: launch_face<FLUX_HLLC>(Dh, u, gettimesteps, gf, s); break;
+	}
+	return cudaGetLastError();
+}
+
 cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int gettimesteps, double *dt, cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
@@ -104,16 +120,7 @@ cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int ge
 			}
 		}
 	}
-	const dim3 gf = grid(D.naface);
-	switch (D.flux) {
-	case FLUX_LLF: launch_face<FLUX_LLF>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_VANLEER: launch_face<FLUX_VANLEER>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_AUSM: launch_face<FLUX_AUSM>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_AUSMPLUS: launch_face<FLUX_AUSMPLUS>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_ROE: launch_face<FLUX_ROE>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_HLL: launch_face<FLUX_HLL>(Dh, u, gettimesteps, gf, s); break;
-	default: launch_face<FLUX_HLLC>(Dh, u, gettimesteps, gf, s); break;
-	}
+	face_launch(Dh, u, gettimesteps, s);
 	nk++;
 	k_gather<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
 	nk++;

@@ -665,3 +665,82 @@ fv_status fv_solver_history(const fv_solver *S, int member, int maxn, double *re
 long long fv_solver_kernels_per_step(const fv_solver *S) { return S ? S->kernels_per_step : 0; }
 
 }  // extern "C"
+
+namespace {
+
+/* compulsory-traffic models (bytes per launch, all batch members) */
+double bytes_model(const fv_solver *S, int which)
+{
+	const fv_disc_impl *D = S->D;
+	const double Nc = D->d.nelem, Nf = D->d.naface, Nb = D->d.nbface, B = D->batch;
+	const bool lim = D->d.recon == FV_REC_BARTHJESPERSEN || D->d.recon == FV_REC_VENKATAKRISHNAN ||
+	                 D->d.recon == FV_REC_WENO;
+	const double w = S->A.prec;
+	const double nblk = Nc + 2 * (Nf - Nb);  // stored blocks
+	switch (which) {
+	case FV_KERNEL_RESIDUAL:
+		if (!D->d.order2) return B * (80 * Nc + 48 * Nf);
+		return B * (lim ? 464 * Nc + 144 * Nf : 304 * Nc + 96 * Nf);
+	case FV_KERNEL_FACE_FLUX:
+		// per cell: primitive state 32, gradients 64, centroid 16 (+ limiter 32);
+		// per face: geometry 48 (l/r 8, n and length 24, centre 16), flux 32 + spectral radii 16 out
+		return B * ((lim ? 144 : 112) * Nc + 96 * Nf);
+	case FV_KERNEL_JACOBIAN:
+		return B * (32 * Nc + 40 * (Nf - Nb) + 48 * Nb + 16 * w * nblk + 4 * nblk);
+	case FV_KERNEL_PRECOND_APPLY:
+		// every stored block once + column indices + r in, z out, intermediate y out and in
+		return B * (16 * w * nblk + 4 * 2 * (Nf - Nb) + 4 * 4 * w * Nc + 2 * 32 * Nc);
+	case FV_KERNEL_SPMV:
+		return B * (16 * w * nblk + 4 * 2 * (Nf - Nb) + 2 * 32 * Nc);
+	case FV_KERNEL_PRECOND_SETUP:
+		return B * (2 * 16 * w * nblk + 16 * w * Nc);
+	}
+	return 0;
+}
+
+}  // namespace
+
+extern "C" fv_status fv_solver_time_kernel(fv_solver *S, const double *u, int which, int reps, double *avg_ms,
+                                           double *bytes)
+{
+	if (!S || !u || reps < 1 || !avg_ms) { set_error("invalid argument"); return FV_ERR_INVALID; }
+	fv_disc_impl *D = S->D;
+	cudaStream_t s = D->stream;
+	const int N = D->d.nelem, B = D->batch;
+	cudaError_t e = cudaSuccess;
+	int nk = 0;
+	// bring every buffer the kernels read into a consistent state at u
+	e = cudaMemsetAsync(S->r, 0, sizeof(double) * 4 * (size_t)N * B, s);
+	if (!e) e = residual_launch(D, u, S->r, 1, S->dtm, s);
+	if (!e) e = jacobian_launch(D, u, S->A, s);
+	if (!e) e = precond_setup(S->P, S->S.pc_err, nullptr, s, &nk);
+	if (e) return cuda_status(e, "timing setup");
+	auto one = [&]() -> cudaError_t {
+		switch (which) {
+		case FV_KERNEL_RESIDUAL: return residual_launch(D, u, S->r, 1, S->dtm, s);
+		case FV_KERNEL_FACE_FLUX: return face_launch(D, u, 1, s);
+		case FV_KERNEL_JACOBIAN: return jacobian_launch(D, u, S->A, s);
+		case FV_KERNEL_PRECOND_APPLY: return precond_apply(S->P, S->r, S->du, nullptr, s, &nk);
+		case FV_KERNEL_SPMV: return block_spmv(S->A, D->d.cnbr, S->r, S->du, nullptr, s, &nk);
+		case FV_KERNEL_PRECOND_SETUP: return precond_setup(S->P, S->S.pc_err, nullptr, s, &nk);
+		}
+		return cudaErrorInvalidValue;
+	};
+	for (int k = 0; k < 3 && !e; k++) e = one();
+	cudaEvent_t a, b;
+	cudaEventCreate(&a);
+	cudaEventCreate(&b);
+	if (!e) e = cudaEventRecord(a, s);
+	for (int k = 0; k < reps && !e; k++) e = one();
+	if (!e) e = cudaEventRecord(b, s);
+	if (!e) e = cudaEventSynchronize(b);
+	float ms = 0;
+	if (!e) e = cudaEventElapsedTime(&ms, a, b);
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	count_launches(nk);
+	if (e) return cuda_status(e, "kernel timing");
+	*avg_ms = ms / reps;
+	if (bytes) *bytes = bytes_model(S, which);
+	return FV_OK;
+}

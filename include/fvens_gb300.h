@@ -113,6 +113,9 @@ fv_status fv_mesh_export(const fv_mesh *m, double *coords, int *nnode, int *inpo
 /* face_lr: naface x 2 (left, right; right = -1-ib on boundary face ib);
  * fnorm: naface x 3 (nx, ny, len); area: nelem; cc: nelem x 2; color: nelem */
 fv_status fv_mesh_geometry(const fv_mesh *m, int *face_lr, double *fnorm, double *area, double *cc, int *color);
+/* block-colour elimination order of the SGS / ILU(0) preconditioners
+ * (compact parts of ~part_size cells, parts coloured): order[position] = cell */
+fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *nparts, int *ncolors);
 void fv_mesh_destroy(fv_mesh *m);
 
 /* ---- spatial discretisation: FlowFV<freal,order2,constVisc> (afactory.cpp:252-276) ---- */
@@ -226,6 +229,17 @@ fv_status fv_solver_solve_host(fv_solver *s, double *h_u, const int *member_mask
 fv_status fv_solver_history(const fv_solver *s, int member, int maxn, double *res, double *cfl, int *linits, int *n);
 /* kernels launched by one pseudo-time step (all members) */
 long long fv_solver_kernels_per_step(const fv_solver *s);
+/* Times one hot-path launch sequence in isolation with CUDA events on the
+ * handle's stream (3 warm-up launches, then reps timed ones) at state d_u;
+ * *avg_ms = mean duration, *bytes = compulsory (algorithmic) bytes of one
+ * launch for the roofline.  Synchronises. */
+#define FV_KERNEL_RESIDUAL 0        /* whole residual evaluation */
+#define FV_KERNEL_FACE_FLUX 1       /* face reconstruction + flux kernel */
+#define FV_KERNEL_JACOBIAN 2        /* Jacobian assembly */
+#define FV_KERNEL_PRECOND_APPLY 3   /* one preconditioner application */
+#define FV_KERNEL_SPMV 4            /* block SpMV */
+#define FV_KERNEL_PRECOND_SETUP 5   /* factorisation */
+fv_status fv_solver_time_kernel(fv_solver *s, const double *d_u, int which, int reps, double *avg_ms, double *bytes);
 
 /* ---- pointwise device evaluations (for validation against the reference) ---- */
 /* n states: d_ul, d_ur n x 4, d_n n x 2 -> d_f n x 4 (condition 0's physics) */

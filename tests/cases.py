@@ -36,7 +36,7 @@ RESIDUAL_CASES = [
      dict(flux="HLLC", gradient="GREENGAUSS", reconstruction="VENKATAKRISHNAN", limiter_param=5.0), NACA_INV_BCS),
     ("llf_wls", channel, dict(Minf=0.5), dict(flux="LLF"), CHANNEL_BCS),
     ("vanleer_wls", channel, dict(Minf=0.5), dict(flux="VANLEER", flux_jac="ROE"), CHANNEL_BCS),
-    ("ausm_wls", channel, dict(Minf=0.5), dict(flux="AUSM"), CHANNEL_BCS),
+    ("ausm_wls", channel, dict(Minf=0.5, aoa_deg=3.0), dict(flux="AUSM"), CHANNEL_BCS),
     ("ausmplus_wls", channel, dict(Minf=0.5), dict(flux="AUSMPLUS", flux_jac="ROE"), CHANNEL_BCS),
     ("hll_wls", channel, dict(Minf=0.5), dict(flux="HLL"), CHANNEL_BCS),
     ("hllc_wls_vanalbada", naca, dict(Minf=0.8, aoa_deg=1.25),

