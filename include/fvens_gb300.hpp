@@ -9,8 +9,6 @@
  *     assemble_jacobian(u, A)                            same, into fvg::BlockJacobian
  *     getGradients(u, grads)                             getGradients
  *   SteadyBackwardEulerSolver::solve (src/ode)          fvg::SteadyBackwardEulerSolver::solve
- *   parse_flow_controlfile (src/utilities/controlparser.cpp)
- *                                                      fvg::parse_flow_controlfile (fvens_control.hpp)
  *
  * Errors become exceptions of the reference's kinds: Numerical_error,
  * Tolerance_error, std::invalid_argument / std::runtime_error.
