@@ -1,15 +1,19 @@
 """Headline benchmark: steady transonic NACA 0012 solves per second on one GB300.
 
 Workload (the reference's transonic inviscid configuration): NACA 0012 with a
-closed trailing edge on a 512 x 256 O-grid to 30 chords (radial growth 1.05,
-outer 40 % of the rings triangulated; 183,296 cells, 314,880 faces), M 0.8,
-AoA 1.25 deg, HLLC flux, Green-Gauss gradients, Venkatakrishnan limiter
-(K = 5).  One step = one complete steady solve from freestream: a first-order
-starter solve followed by the second-order solve to an absolute area-weighted
-energy-residual norm below 1e-10, with the FP32 stored Jacobian and the FP32
-block-colour ILU(0) preconditioner inside FGMRES(30).  Synthetic mesh and
-inputs (seeded generator); the working set (states, Jacobian, Krylov basis,
-~0.5 GB) exceeds the 126 MB L2, so no explicit flush is needed.
+closed trailing edge on a 512 x 256 O-grid to 30 chords (outer 40 % of the
+rings triangulated; 183,296 cells, 314,880 faces), M 0.8, AoA 1.25 deg, HLLC
+flux, Green-Gauss gradients, Venkatakrishnan limiter (K = 5).  The radial
+spacing grows by 1.02 per ring (first cell 3.8e-3 chords): with growth 1.05
+the first cell is 5.7e-6 chords and the reference's pseudo-time method does
+not reach 1e-10 on it in thousands of steps.  One step = one complete steady
+solve from freestream: a first-order starter (100 pseudo-time steps) followed
+by the second-order solve to an absolute area-weighted energy-residual norm
+below 1e-10, matrix-free FP64 Jacobian-vector products in FGMRES(30) with the
+FP32 stored first-order Jacobian and the FP32 block-colour ILU(0)
+preconditioner.  Synthetic mesh and inputs (seeded generator); the working set
+(states, Jacobian, Krylov basis, ~0.5 GB) exceeds the 126 MB L2, so no
+explicit flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -30,17 +34,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-MESH = [512, 256, 30.0, 0, 0, 1.05, 154, 3]
+MESH = [512, 256, 30.0, 0, 0, 1.02, 154, 3]
 PHYS = dict(Minf=0.8, aoa_deg=1.25)
 NUM_MAIN = dict(flux="HLLC", gradient="GREENGAUSS", reconstruction="VENKATAKRISHNAN", limiter_param=5.0)
 NUM_START = dict(flux="HLLC", gradient="NONE")
 BCS = [(2, "slipwall", ()), (4, "farfield", ())]
-STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=1,
-               min_relax=0.3)
-MAIN = dict(cfl_min=50, cfl_max=1000, tolerance=1e-10, abs_tolerance=1, max_timesteps=600, nl_update=1,
-            min_relax=0.3, pc="ilu0")
-WORKLOAD = "naca0012_transonic_512x256_ogrid_hllc_gg_venkat5"
-METRIC = "solves/s to ||R||<1e-10 (transonic NACA0012, FP32 Jacobian + FP32 block-colour ILU0)"
+STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
+               min_relax=0.2, pc="ilu0")
+MAIN = dict(cfl_min=50, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
+            min_relax=0.2, pc="ilu0", matrix_free=1)
+WORKLOAD = "naca0012_transonic_512x256_ogrid_g1.02_hllc_gg_venkat5"
+METRIC = "solves/s to ||R||<1e-10 (transonic NACA0012, matrix-free FGMRES, FP32 Jacobian + FP32 block-colour ILU0)"
 
 
 def _dist():
@@ -128,9 +132,9 @@ def run_ours(args):
 
     def solve_device():
         ud.copy_(u0d)
-        S1.solve(ud, raise_on_error=False)
-        rc, st = S2.solve(ud, raise_on_error=False)
-        return rc, st
+        _, st1 = S1.solve(ud, raise_on_error=False)
+        rc, st2 = S2.solve(ud, raise_on_error=False)
+        return st1[0], st2[0]
 
     def barrier():
         if world > 1:
@@ -138,7 +142,7 @@ def run_ours(args):
             dist.barrier()
 
     for _ in range(args.warmup):
-        rc, st = solve_device()
+        solve_device()
     torch.cuda.synchronize()
     launches0 = fv.kernel_launch_count()
     barrier()
@@ -148,8 +152,7 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         ev0.record()
         for _ in range(args.steps):
-            rc, st = solve_device()
-            stats.append(st[0])
+            stats.append(solve_device())
         ev1.record()
         torch.cuda.synchronize()
     barrier()
@@ -161,6 +164,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * args.steps / (ms / 1e3)
+    converged = all(s2["status"] == 0 for _, s2 in stats)
 
     # end to end through the host-buffer C-ABI call: pinned host state in,
     # converged state out (starter and main solve)
@@ -181,20 +185,29 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * args.steps / e2e_s
+    cl = main.surface_data(ud, 2)[0]
 
-    # per-kernel timing (roofline) at the converged state
-    def timed(which, reps=20):
+    # per-kernel timing (roofline) at the converged state; time shares of one
+    # solve from the launch counts per step / per Krylov iteration
+    def timed(S, which, reps=20):
         import ctypes
         a, b = ctypes.c_double(), ctypes.c_double()
-        fv.check(fv.lib().fv_solver_time_kernel(S2._h, fv._vp(fv.dptr(ud)), which, reps, ctypes.byref(a),
+        fv.check(fv.lib().fv_solver_time_kernel(S._h, fv._vp(fv.dptr(ud)), which, reps, ctypes.byref(a),
                                                 ctypes.byref(b)))
         return a.value, b.value
 
     kern = {}
     for name, which in (("residual", 0), ("face_flux", 1), ("jacobian", 2), ("ilu0_apply", 3), ("spmv", 4),
                         ("ilu0_setup", 5)):
-        ms_k, by = timed(which)
+        ms_k, by = timed(S2, which)
         kern[name] = dict(ms=ms_k, bytes=by, gbs=by / (ms_k * 1e-3) / 1e9)
+    s1, s2 = stats[-1]
+    steps_main, lin_main = s2["steps"], s2["lin_iters"]
+    mf = MAIN.get("matrix_free", 0)
+    calls = {"residual": steps_main + (lin_main if mf else 0), "jacobian": steps_main, "ilu0_setup": steps_main,
+             "ilu0_apply": lin_main, "spmv": 0 if mf else lin_main}
+    share_ms = {k: calls[k] * kern[k]["ms"] for k in calls}
+    dom = max(share_ms, key=share_ms.get)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -202,9 +215,6 @@ def run_ours(args):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    dom = "ilu0_apply"
-    steps_main = statistics.median([s["steps"] for s in stats])
-    lin_main = statistics.median([s["lin_iters"] for s in stats])
     nf = m.naface
     nblocks = m.nelem + 2 * (m.naface - m.nbface)
     line = {
@@ -218,28 +228,29 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 residual / f32 jacobian+ilu0" if prec == 4 else "f64",
+        "dtype": "f64 residual+krylov / f32 jacobian+ilu0" if prec == 4 else "f64",
         "data": "synthetic (seeded NACA 0012 O-grid generator, freestream start)",
         "config": {"workload": WORKLOAD, "cells": m.nelem, "faces": nf, "batch": 1,
                    "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": "working set > L2 (no flush needed)",
-                   "main_steps_median": steps_main, "linear_iters_median": lin_main,
-                   "converged": all(s["status"] == 0 for s in stats),
-                   "final_res_max": max(s["res"] for s in stats)},
-        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": 2 * u0.nbytes,
-                "d2h_bytes_per_step": 2 * u0.nbytes},
+                   "starter_steps": s1["steps"], "main_steps": steps_main, "linear_iters": lin_main,
+                   "converged": converged, "final_res": s2["res"],
+                   "cl_cdp": [float(cl[0]), float(cl[1])]},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(u0.nbytes),
+                "d2h_bytes_per_step": int(u0.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": hbm_peak,
                      "unit": "GB/s", "frac": kern[dom]["gbs"] / hbm_peak, "traffic": None,
                      "peak_source": peak_src},
         "kernels": kern,
+        "solve_time_shares_ms": share_ms,
         "residual_gfaces_s": nf / (kern["residual"]["ms"] * 1e-3) / 1e9,
         "jacobian_blocks_s": nblocks / (kern["jacobian"]["ms"] * 1e-3),
         "ilu0_sweep_gbs": kern["ilu0_apply"]["gbs"],
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(m, steps_main, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(m, s1, s2, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -247,30 +258,55 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(m, steps_per_solve, budget_s):
-    """The oracle (the CPU restatement of the reference's path) on the host
-    cores: a bounded number of pseudo-time steps of the same second-order
-    solve, scaled to solves/s with the GPU's step count per solve."""
+def _oracle_case(m):
+    from oracle import orc
+    om = orc.Mesh.from_export(m.export())
+    od1 = orc.Disc(om, **PHYS, **NUM_START, bcs=BCS)
+    od2 = orc.Disc(om, **PHYS, **NUM_MAIN, bcs=BCS)
+    return od1, od2
+
+
+def _oracle_steps(od, cfg, u, nsteps, lin_maxit):
+    """nsteps pseudo-time steps on the oracle with every linear solve running
+    exactly lin_maxit FGMRES iterations (relative tolerance out of reach)."""
+    t0 = time.perf_counter()
+    od.steady_solve(u, cflmin=cfg["cfl_min"], cflmax=cfg["cfl_max"], tol=1e-30, maxiter=nsteps, pc="ilu0",
+                    matrix_free=bool(cfg.get("matrix_free", 0)), nl_update="bounded", min_relax=cfg["min_relax"],
+                    abs_tol=True, lin_rtol=1e-14, lin_maxit=lin_maxit)
+    return (time.perf_counter() - t0) / nsteps
+
+
+def _oracle_step_model(od, cfg, u, budget_s):
+    """Per-step and per-Krylov-iteration cost of the oracle: timed steps with 1
+    and with 8 FGMRES iterations each, fitted to t = a + b * iterations."""
+    t1 = _oracle_steps(od, cfg, u, 1, 1)
+    n = max(1, min(10, int(0.25 * budget_s / max(t1, 1e-3))))
+    t1 = _oracle_steps(od, cfg, u, n, 1)
+    t8 = _oracle_steps(od, cfg, u, n, 8)
+    b = max((t8 - t1) / 7.0, 0.0)
+    return t1 - b, b, n
+
+
+def cpu_baseline(m, starter, main, budget_s):
+    """The oracle (the CPU restatement of the reference's path, natural-order
+    ILU(0) as PETSc's) on the host cores: a bounded sample of pseudo-time
+    steps of the starter and of the main solve with pinned FGMRES iteration
+    counts gives the cost per step and per Krylov iteration, which is applied
+    to the step and iteration counts of the GPU solve.  starter / main: the
+    GPU's fv_solve_stats of the two solves."""
     from oracle import orc
     nthreads = os.cpu_count() or 1
     orc.set_threads(nthreads)
-    om = orc.Mesh.from_export(m.export())
-    od = orc.Disc(om, **PHYS, **NUM_MAIN, bcs=BCS)
-    u0 = np.tile(od.freestream(), (m.nelem, 1))
-    nsteps = 1
-    t0 = time.perf_counter()
-    od.steady_solve(u0, cflmin=MAIN["cfl_min"], cflmax=MAIN["cfl_max"], tol=1e-10, maxiter=nsteps, pc="ilu0",
-                    nl_update="robust_flow", min_relax=MAIN["min_relax"])
-    per = time.perf_counter() - t0
-    nsteps = max(1, min(20, int(budget_s / max(per, 1e-3))))
-    t0 = time.perf_counter()
-    od.steady_solve(u0, cflmin=MAIN["cfl_min"], cflmax=MAIN["cfl_max"], tol=1e-10, maxiter=nsteps, pc="ilu0",
-                    nl_update="robust_flow", min_relax=MAIN["min_relax"])
-    per = (time.perf_counter() - t0) / nsteps
-    value = 1.0 / (per * max(steps_per_solve, 1))
-    return {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
-            "sample": f"{nsteps} second-order implicit pseudo-time steps of the same workload on the oracle "
-                      f"({per:.2f} s/step, natural-order ILU0, FGMRES(30)), scaled by {steps_per_solve} steps/solve"}
+    od1, od2 = _oracle_case(m)
+    u0 = np.tile(od2.freestream(), (m.nelem, 1))
+    a1, b1, n1 = _oracle_step_model(od1, STARTER, u0, 0.4 * budget_s)
+    a2, b2, n2 = _oracle_step_model(od2, MAIN, u0, 0.6 * budget_s)
+    solve_s = (a1 * starter["steps"] + b1 * starter["lin_iters"]) + (a2 * main["steps"] + b2 * main["lin_iters"])
+    return {"value": 1.0 / solve_s, "unit": "solves/s", "cores": nthreads, "kind": "port",
+            "sample": f"2 x {n1} starter + 2 x {n2} main pseudo-time steps of the same workload on the oracle with "
+                      f"1 and 8 FGMRES(30) iterations per step (natural-order ILU(0)); per step {a1:.3f} / {a2:.3f} s "
+                      f"+ per Krylov iteration {b1:.3f} / {b2:.3f} s, applied to {starter['steps']} + {main['steps']} "
+                      f"steps and {starter['lin_iters']} + {main['lin_iters']} Krylov iterations per solve"}
 
 
 def run_reference(args):
@@ -287,10 +323,11 @@ def run_reference(args):
     if not os.path.exists(fv.LIB_PATH):
         fvbuild.build_library()
     m = fv.UMesh.generate(fv.MESH_NACA_OGRID, MESH, reorder=1)
-    steps_per_solve = args.ref_steps_per_solve
     vals = []
     for k in range(args.warmup + args.steps):
-        cb = cpu_baseline(m, steps_per_solve, args.cpu_seconds / max(args.steps + args.warmup, 1))
+        cb = cpu_baseline(m, {"steps": STARTER["max_timesteps"], "lin_iters": args.ref_starter_iters},
+                          {"steps": args.ref_steps_per_solve, "lin_iters": args.ref_iters_per_solve},
+                          args.cpu_seconds / max(args.steps + args.warmup, 1))
         if k >= args.warmup:
             vals.append(cb)
     value = statistics.median([v["value"] for v in vals])
@@ -308,14 +345,23 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain", action="store_true", help="FP64 Jacobian and preconditioner (the plain path)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--max-main-steps", type=int, default=0,
+                    help="profiling aid: cap the main solve's pseudo-time steps (the solve then does not converge)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--ref-steps-per-solve", type=int, default=150)
+    ap.add_argument("--ref-steps-per-solve", type=int, default=1100,
+                    help="main-solve pseudo-time steps per solve assumed by the reference arm")
+    ap.add_argument("--ref-iters-per-solve", type=int, default=26000,
+                    help="main-solve Krylov iterations per solve assumed by the reference arm")
+    ap.add_argument("--ref-starter-iters", type=int, default=1800,
+                    help="starter Krylov iterations per solve assumed by the reference arm")
     args = ap.parse_args()
+    if args.max_main_steps > 0:
+        MAIN["max_timesteps"] = args.max_main_steps
     if args.impl == "reference":
         run_reference(args)
     else:

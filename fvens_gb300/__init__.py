@@ -225,6 +225,13 @@ class FlowFV:
     def assemble_jacobian(self, u, matrix):
         check(lib().fv_assemble_jacobian(self._h, _vp(dptr(u)), matrix._h))
 
+    def surface_data(self, u, wall_marker):
+        """(Cl, CDp, CDsf) over the faces of wall_marker, one row per batch member
+        (FlowFV_base::computeSurfaceData)."""
+        out = np.zeros((self.batch, 3))
+        check(lib().fv_surface_data(self._h, _vp(dptr(u)), int(wall_marker), _hp(out, ctypes.c_double)))
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None) is not None and _lib is not None:
             _lib.fv_disc_destroy(self._h)
@@ -324,7 +331,7 @@ def solver_cfg(**kw):
         if k == "pc":
             c.pc_type = PC[v]
         elif k == "nl_update" and isinstance(v, str):
-            c.nl_update = 0 if v == "full" else 1
+            c.nl_update = {"full": 0, "robust_flow": 1, "bounded": 2}[v]
         elif k in names:
             setattr(c, k, v)
         else:

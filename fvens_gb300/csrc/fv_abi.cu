@@ -311,6 +311,8 @@ fv_status fv_disc_create(fv_mesh *m, const fv_physics_cfg *phys, int batch, cons
 	if (!e) e = dalloc(&w.phi, B * ne, own);
 	if (!e) e = dalloc(&w.fflux, B * nf, own);
 	if (!e) e = dalloc(&w.spec, B * nf, own);
+	if (!e) e = dupload(&D->btag, nb > 0 ? h.btag : std::vector<int>(1, 0), own);
+	if (!e) e = dalloc(&D->surf, 4 * B, own);
 	if (e) {
 		st = cuda_status(e, "discretisation setup");
 		fv_disc_destroy(D);

@@ -105,6 +105,8 @@ struct fv_disc_impl {
 	// owned device arrays
 	std::vector<void *> owned;
 	ResidualWork w;
+	int *btag = nullptr;       // device: boundary marker of each boundary face
+	double *surf = nullptr;    // device: surface-integral partials [batch][4]
 	cudaStream_t stream = 0;
 	int kernels_launched = 0;  // running count of this handle's kernel launches
 };

@@ -191,26 +191,6 @@ __global__ void __launch_bounds__(BS) k_ilu_colour(int nelem, int p0, int p1, co
 	ilu_row<R, RA>(nelem, p, b, A, pos_cell, pnbr, pnbrpos, F, Dinv, err);
 }
 
-/* parts of one block colour: one CTA per part, levels separated by barriers */
-template <class R, class RA>
-__global__ void __launch_bounds__(BS) k_ilu_parts(int nelem, int part0, const int *__restrict__ part_ptr,
-                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
-                                                  const RA *__restrict__ A, const int *__restrict__ pos_cell,
-                                                  const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
-                                                  R *__restrict__ F, R *__restrict__ Dinv, int *err, const int *active)
-{
-	const int b = blockIdx.y;
-	if (member_off(active, b)) return;
-	const int part = part0 + blockIdx.x;
-	const int pend = part_ptr[part + 1];
-	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-	for (int l = l0; l < l1; l++) {
-		const int e = l + 1 < l1 ? lev_pos[l + 1] : pend;
-		for (int p = lev_pos[l] + threadIdx.x; p < e; p += BS) ilu_row<R, RA>(nelem, p, b, A, pos_cell, pnbr, pnbrpos, F, Dinv, err);
-		__syncthreads();
-	}
-}
-
 /* forward sweep of one colour: y_p = r_i - sum_{lower} L y  (ILU) or
  * Dinv (r_i - sum_{lower} A y) (SGS) */
 template <class R>
@@ -256,25 +236,6 @@ __global__ void __launch_bounds__(BS) k_fwd(int nelem, int p0, int p1, int sgs, 
 	const int p = p0 + blockIdx.x * BS + threadIdx.x;
 	if (p >= p1 || member_off(active, b)) return;
 	fwd_row<R>(nelem, p, b, sgs, r, pos_cell, pnbrpos, F, Dinv, y);
-}
-
-template <class R>
-__global__ void __launch_bounds__(BS) k_fwd_parts(int nelem, int part0, const int *__restrict__ part_ptr,
-                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
-                                                  int sgs, const double *__restrict__ r, const int *__restrict__ pos_cell,
-                                                  const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
-                                                  const R *__restrict__ Dinv, R *__restrict__ y, const int *active)
-{
-	const int b = blockIdx.y;
-	if (member_off(active, b)) return;
-	const int part = part0 + blockIdx.x;
-	const int pend = part_ptr[part + 1];
-	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-	for (int l = l0; l < l1; l++) {
-		const int e = l + 1 < l1 ? lev_pos[l + 1] : pend;
-		for (int p = lev_pos[l] + threadIdx.x; p < e; p += BS) fwd_row<R>(nelem, p, b, sgs, r, pos_cell, pnbrpos, F, Dinv, y);
-		__syncthreads();
-	}
 }
 
 /* backward sweep of one colour: z_i = Dinv (y_p - sum_{upper} U z) (ILU) or
@@ -328,25 +289,305 @@ __global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, 
 	bwd_row<R>(nelem, p, b, sgs, pos_cell, pnbr, pnbrpos, F, Dinv, y, z);
 }
 
-/* backward sweep of the parts of one block colour: levels in reverse (a cell's
- * upper neighbours inside its part sit on higher forward levels) */
+/* ---- block-colour sweeps: one warp per part, the part staged in shared memory ----
+ *
+ * A part's cells occupy the contiguous elimination positions [p0, p1), sorted
+ * by dependency level.  Phase 1 (all lanes, coalesced) folds the contributions
+ * of neighbours outside the part -- finished by earlier colour launches -- into
+ * a right-hand side and copies the blocks that couple the part to itself into
+ * shared memory; phase 2 walks the levels with four lanes per cell (one block
+ * row each) reading shared memory only; phase 3 writes the part back.  The
+ * dependency chain of a part therefore costs shared-memory latency per level,
+ * not global-memory latency. */
+constexpr int PW = 32;  // lanes per part CTA: 8 cells x 4 block rows per pass
+
+/* dynamic shared memory of the sweep kernels for parts of at most cap cells */
 template <class R>
-__global__ void __launch_bounds__(BS) k_bwd_parts(int nelem, int part0, const int *__restrict__ part_ptr,
+size_t sweep_smem(int cap) { return (size_t)cap * (64 + 16 + 4 + 4) * sizeof(R) + (size_t)cap * sizeof(int4); }
+/* ... and of the factorisation */
+template <class R>
+size_t ilu_smem(int cap) { return (size_t)cap * (80 + 16) * sizeof(R); }
+
+template <class R>
+__device__ __forceinline__ R dot4(const R *a, const R *v) { return a[0] * v[0] + a[1] * v[1] + a[2] * v[2] + a[3] * v[3]; }
+
+/* forward sweep of the parts of one colour: y_p = r_i - sum_{lower} L y (ILU)
+ * or Dinv (r_i - sum_{lower} A y) (SGS) */
+template <class R>
+__global__ void __launch_bounds__(PW) k_fwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
+                                                  int sgs, const double *__restrict__ r, const int *__restrict__ pos_cell,
+                                                  const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
+                                                  const R *__restrict__ Dinv, R *__restrict__ y, const int *active)
+{
+	extern __shared__ __align__(16) unsigned char smem[];
+	R *sF = reinterpret_cast<R *>(smem);  // [cap][4][16] in-part lower blocks
+	R *sD = sF + (size_t)cap * 64;         // [cap][16]    Dinv (SGS)
+	R *sv = sD + (size_t)cap * 16;         // [cap][4]     y of the part
+	R *st = sv + (size_t)cap * 4;          // [cap][4]     right-hand side
+	int4 *snb = reinterpret_cast<int4 *>(st + (size_t)cap * 4);  // in-part lower neighbours (local), -1 none
+	const int b = blockIdx.y;
+	if (member_off(active, b)) return;
+	const int part = part0 + blockIdx.x;
+	const int p0 = part_ptr[part], p1 = part_ptr[part + 1], n = p1 - p0;
+	const size_t N = nelem;
+	const R *Fb = F + (size_t)b * 5 * N * 16;
+	R *yb = y + (size_t)b * N * 4;
+	const double4 *rb = reinterpret_cast<const double4 *>(r + (size_t)b * N * 4);
+	const int lane = threadIdx.x;
+	for (int c = lane; c < n; c += PW) {
+		const int p = p0 + c;
+		const double4 rv = rb[pos_cell[p]];
+		R s[4] = {R(rv.x), R(rv.y), R(rv.z), R(rv.w)};
+		const int4 np4 = pnbrpos[p];
+		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+		int loc[4];
+		for (int j = 0; j < 4; j++) {
+			loc[j] = -1;
+			const int q = nbp[j];
+			if (q < 0 || q >= p) continue;
+			R blk[16];
+			load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
+			if (q >= p0) {
+				loc[j] = q - p0;
+				store_blk(sF + ((size_t)c * 4 + j) * 16, blk);
+			} else {
+				const R yy[4] = {yb[4 * (size_t)q], yb[4 * (size_t)q + 1], yb[4 * (size_t)q + 2], yb[4 * (size_t)q + 3]};
+				R t[4];
+				mv(blk, yy, t);
+				for (int k = 0; k < 4; k++) s[k] -= t[k];
+			}
+		}
+		for (int k = 0; k < 4; k++) st[4 * c + k] = s[k];
+		snb[c] = make_int4(loc[0], loc[1], loc[2], loc[3]);
+		if (sgs) {
+			R d[16];
+			load_blk(Dinv + ((size_t)b * N + p) * 16, d);
+			store_blk(sD + (size_t)c * 16, d);
+		}
+	}
+	__syncwarp();
+	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+	const int g = lane >> 2, row = lane & 3;
+	for (int l = l0; l < l1; l++) {
+		const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
+		for (int c0 = ls; c0 < le; c0 += PW / 4) {
+			const int c = c0 + g;
+			const bool on = c < le;
+			R acc = R(0);
+			if (on) {
+				acc = st[4 * c + row];
+				const int4 nb = snb[c];
+				const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
+				for (int j = 0; j < 4; j++)
+					if (l4[j] >= 0) acc -= dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+			}
+			if (sgs) {
+				if (on) st[4 * c + row] = acc;
+				__syncwarp();
+				if (on) acc = dot4(sD + (size_t)c * 16 + 4 * row, st + 4 * c);
+			}
+			if (on) sv[4 * c + row] = acc;
+		}
+		__syncwarp();
+	}
+	for (int e = lane; e < 4 * n; e += PW) yb[(size_t)p0 * 4 + e] = sv[e];
+}
+
+/* backward sweep of the parts of one colour (levels in reverse):
+ * z_i = Dinv (y_p - sum_{upper} U z) (ILU) or y_p - Dinv sum_{upper} A z (SGS) */
+template <class R>
+__global__ void __launch_bounds__(PW) k_bwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
                                                   const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
                                                   const R *__restrict__ Dinv, const R *__restrict__ y,
                                                   double *__restrict__ z, const int *active)
 {
+	extern __shared__ __align__(16) unsigned char smem[];
+	R *sF = reinterpret_cast<R *>(smem);  // [cap][4][16] in-part upper blocks
+	R *sD = sF + (size_t)cap * 64;         // [cap][16]    Dinv
+	R *sv = sD + (size_t)cap * 16;         // [cap][4]     z of the part
+	R *st = sv + (size_t)cap * 4;          // [cap][4]     right-hand side (ILU) / outside sum (SGS)
+	int4 *snb = reinterpret_cast<int4 *>(st + (size_t)cap * 4);
 	const int b = blockIdx.y;
 	if (member_off(active, b)) return;
 	const int part = part0 + blockIdx.x;
-	const int pend = part_ptr[part + 1];
+	const int p0 = part_ptr[part], p1 = part_ptr[part + 1], n = p1 - p0;
+	const size_t N = nelem;
+	const R *Fb = F + (size_t)b * 5 * N * 16;
+	const R *yb = y + (size_t)b * N * 4;
+	double *zb = z + (size_t)b * N * 4;
+	const int lane = threadIdx.x;
+	for (int c = lane; c < n; c += PW) {
+		const int p = p0 + c;
+		const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
+		const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+		R s[4] = {R(0), R(0), R(0), R(0)};
+		int loc[4];
+		for (int j = 0; j < 4; j++) {
+			loc[j] = -1;
+			const int q = nbp[j];
+			if (q < 0 || q <= p) continue;
+			R blk[16];
+			load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
+			if (q < p1) {
+				loc[j] = q - p0;
+				store_blk(sF + ((size_t)c * 4 + j) * 16, blk);
+			} else {
+				const double4 zz = reinterpret_cast<const double4 *>(zb)[nbc[j]];
+				const R zv[4] = {R(zz.x), R(zz.y), R(zz.z), R(zz.w)};
+				R t[4];
+				mv(blk, zv, t);
+				for (int k = 0; k < 4; k++) s[k] += t[k];
+			}
+		}
+		const R *yp = yb + ((size_t)p) * 4;
+		for (int k = 0; k < 4; k++) st[4 * c + k] = sgs ? s[k] : yp[k] - s[k];
+		if (sgs)
+			for (int k = 0; k < 4; k++) sv[4 * c + k] = yp[k];  // y kept beside the sum until the cell's level
+		snb[c] = make_int4(loc[0], loc[1], loc[2], loc[3]);
+		R d[16];
+		load_blk(Dinv + ((size_t)b * N + p) * 16, d);
+		store_blk(sD + (size_t)c * 16, d);
+	}
+	__syncwarp();
 	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+	const int g = lane >> 2, row = lane & 3;
 	for (int l = l1 - 1; l >= l0; l--) {
-		const int e = l + 1 < l1 ? lev_pos[l + 1] : pend;
-		for (int p = lev_pos[l] + threadIdx.x; p < e; p += BS) bwd_row<R>(nelem, p, b, sgs, pos_cell, pnbr, pnbrpos, F, Dinv, y, z);
-		__syncthreads();
+		const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
+		for (int c0 = ls; c0 < le; c0 += PW / 4) {
+			const int c = c0 + g;
+			const bool on = c < le;
+			R acc = R(0);
+			if (on) {
+				const int4 nb = snb[c];
+				const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
+				for (int j = 0; j < 4; j++)
+					if (l4[j] >= 0) acc += dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+				// ILU: t = (y - outside) - inside;  SGS: t = outside + inside
+				acc = sgs ? st[4 * c + row] + acc : st[4 * c + row] - acc;
+				st[4 * c + row] = acc;
+			}
+			__syncwarp();
+			if (on) {
+				const R dz = dot4(sD + (size_t)c * 16 + 4 * row, st + 4 * c);
+				sv[4 * c + row] = sgs ? sv[4 * c + row] - dz : dz;
+			}
+		}
+		__syncwarp();
+	}
+	for (int c = lane; c < n; c += PW) {
+		const R *v = sv + 4 * c;
+		reinterpret_cast<double4 *>(zb)[pos_cell[p0 + c]] = make_double4(double(v[0]), double(v[1]), double(v[2]), double(v[3]));
+	}
+}
+
+/* block ILU(0) of the parts of one colour, rows staged in shared memory:
+ * row p (IKJ, no fill) is final once every lower neighbour's row is; four
+ * lanes per row, lane q owning block row q of every block of the row. */
+template <class R, class RA>
+__global__ void __launch_bounds__(PW) k_ilu_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+                                                  const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
+                                                  const RA *__restrict__ A, const int *__restrict__ pos_cell,
+                                                  const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
+                                                  R *__restrict__ F, R *__restrict__ Dinv, int *err, const int *active)
+{
+	extern __shared__ __align__(16) unsigned char smem[];
+	R *sRow = reinterpret_cast<R *>(smem);  // [cap][5][16]
+	R *sD = sRow + (size_t)cap * 80;         // [cap][16] inverted factored diagonal
+	const int b = blockIdx.y;
+	if (member_off(active, b)) return;
+	const int part = part0 + blockIdx.x;
+	const int p0 = part_ptr[part], p1 = part_ptr[part + 1], n = p1 - p0;
+	const size_t N = nelem;
+	const RA *Ab = A + (size_t)b * 5 * N * 16;
+	R *Fb = F + (size_t)b * 5 * N * 16;
+	R *Db = Dinv + (size_t)b * N * 16;
+	const int lane = threadIdx.x;
+	for (int e = lane; e < n * 5; e += PW) {
+		const int s = e / n, c = e - s * n;
+		RA tmp[16];
+		R blk[16];
+		load_blk(Ab + ((size_t)s * N + pos_cell[p0 + c]) * 16, tmp);
+		for (int q = 0; q < 16; q++) blk[q] = R(tmp[q]);
+		store_blk(sRow + ((size_t)c * 5 + s) * 16, blk);
+	}
+	__syncwarp();
+	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+	const int g = lane >> 2, row = lane & 3;
+	for (int l = l0; l < l1; l++) {
+		const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
+		for (int c0 = ls; c0 < le; c0 += PW / 4) {
+			const int c = c0 + g;
+			const bool on = c < le;
+			if (on) {
+				const int p = p0 + c;
+				const int icell = pos_cell[p];
+				R *rw = sRow + (size_t)c * 80;
+				const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
+				const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+				const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+				int ord[4], nl = 0;
+				for (int j = 0; j < 4; j++)
+					if (nbp[j] >= 0 && nbp[j] < p) ord[nl++] = j;
+				for (int a = 1; a < nl; a++)
+					for (int d = a; d > 0 && nbp[ord[d]] < nbp[ord[d - 1]]; d--) { const int t = ord[d]; ord[d] = ord[d - 1]; ord[d - 1] = t; }
+				for (int a = 0; a < nl; a++) {
+					const int jk = ord[a], pk = nbp[jk];
+					const bool inpart = pk >= p0;
+					const R *dk;  // inverted diagonal of row k
+					R dkg[16];
+					if (inpart) dk = sD + (size_t)(pk - p0) * 16;
+					else { load_blk(Db + (size_t)pk * 16, dkg); dk = dkg; }
+					// L_ik = A_ik Dinv_k : lane row computes block row `row`
+					R Lr[4];
+					R *aik = rw + (1 + jk) * 16 + 4 * row;
+					for (int m = 0; m < 4; m++) Lr[m] = aik[0] * dk[m] + aik[1] * dk[4 + m] + aik[2] * dk[8 + m] + aik[3] * dk[12 + m];
+					for (int m = 0; m < 4; m++) aik[m] = Lr[m];
+					const int4 kn4 = pnbr[pk];
+					const int kn[4] = {kn4.x, kn4.y, kn4.z, kn4.w};
+					for (int s = 0; s < 5; s++) {
+						const int colcell = s == 0 ? icell : nbc[s - 1];
+						const int colpos = s == 0 ? p : nbp[s - 1];
+						if (colpos < 0 || colpos <= pk) continue;
+						int ks = -1;
+						for (int t = 0; t < 4; t++)
+							if (kn[t] == colcell) ks = t;
+						if (ks < 0) continue;
+						const R *ukj;
+						R ug[16];
+						if (inpart) ukj = sRow + ((size_t)(pk - p0) * 5 + 1 + ks) * 16;
+						else { load_blk(Fb + ((size_t)(1 + ks) * N + pk) * 16, ug); ukj = ug; }
+						R *ais = rw + s * 16 + 4 * row;
+						for (int m = 0; m < 4; m++) ais[m] -= Lr[0] * ukj[m] + Lr[1] * ukj[4 + m] + Lr[2] * ukj[8 + m] + Lr[3] * ukj[12 + m];
+					}
+				}
+			}
+			__syncwarp();
+			if (on) {
+				R dblk[16], inv[16];
+				for (int q = 0; q < 16; q++) dblk[q] = sRow[(size_t)c * 80 + q];
+				if (!inv4(dblk, inv)) {
+					if (row == 0) atomicOr(err, 1);
+					for (int q = 0; q < 16; q++) inv[q] = R(0);
+				}
+				for (int m = 0; m < 4; m++) sD[(size_t)c * 16 + 4 * row + m] = inv[4 * row + m];
+			}
+			__syncwarp();
+		}
+	}
+	for (int e = lane; e < n * 5; e += PW) {
+		const int s = e / n, c = e - s * n;
+		R blk[16];
+		for (int q = 0; q < 16; q++) blk[q] = sRow[((size_t)c * 5 + s) * 16 + q];
+		store_blk(Fb + ((size_t)s * N + p0 + c) * 16, blk);
+	}
+	for (int e = lane; e < n; e += PW) {
+		R blk[16];
+		for (int q = 0; q < 16; q++) blk[q] = sD[(size_t)e * 16 + q];
+		store_blk(Db + ((size_t)p0 + e) * 16, blk);
 	}
 }
 
@@ -408,10 +649,10 @@ __global__ void __launch_bounds__(BS) k_spmv(int nelem, const R *__restrict__ A,
 __global__ void __launch_bounds__(RBS) k_dot_partial(int n, int nblk, const double *__restrict__ a, size_t astride,
                                                      size_t aistride, const double *__restrict__ w, size_t wstride,
                                                      double *__restrict__ part, int slot0, int pstride,
-                                                     const int *active)
+                                                     const int *active, const int *ilim)
 {
 	const int b = blockIdx.y, i = blockIdx.z;
-	if (member_off(active, b)) return;
+	if (member_off(active, b) || (ilim && i > *ilim)) return;
 	const double *av = a + (size_t)b * astride + (size_t)i * aistride;
 	const double *wv = w + (size_t)b * wstride;
 	double s = 0;
@@ -449,47 +690,81 @@ __global__ void k_gm_init(Krylov K, int nblk, double rtol, const int *member_act
 		K.active[b] = on ? 1 : 0;
 		K.iters[b] = 0;
 		K.kdone[b] = 0;
+		if (b == 0) *K.jcur = 0;
 		double *g = K.g + (size_t)b * (K.restart + 1);
 		for (int k = 0; k <= K.restart; k++) g[k] = 0;
 		g[0] = bn;
 	}
 }
 
-/* v = scal * a for active members (scal = K.scal[b][idx]) */
-__global__ void k_scale(size_t n, const double *__restrict__ a, size_t astride, double *__restrict__ v, size_t vstride,
-                        const double *__restrict__ scal, int idx, const int *active, int zero_x_of, double *x)
+/* v0 = vcur = b / ||b|| for active members; x := 0 */
+__global__ void k_first_basis(Krylov K, const double *__restrict__ bvec, double *__restrict__ x)
 {
 	const int b = blockIdx.y;
+	const size_t n = K.n;
 	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= n) return;
-	if (zero_x_of && x) x[(size_t)b * n + e] = 0.0;
-	if (member_off(active, b)) return;
-	v[(size_t)b * vstride + e] = scal[8 * b + idx] * a[(size_t)b * astride + e];
+	if (x) x[(size_t)b * n + e] = 0.0;
+	if (!K.active[b]) return;
+	const double v = K.scal[8 * b + 3] * bvec[(size_t)b * n + e];
+	K.V[(size_t)b * n + e] = v;
+	K.vcur[(size_t)b * n + e] = v;
+}
+
+/* v_{j+1} = vcur = w / h_{j+1,j} for members still iterating */
+__global__ void k_next_basis(Krylov K)
+{
+	const int b = blockIdx.y;
+	const size_t n = K.n;
+	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= n || !K.active[b]) return;
+	const int j = *K.jcur;
+	const double v = K.scal[8 * b + 2] * K.w[(size_t)b * n + e];
+	K.V[((size_t)(j + 1) * K.batch + b) * n + e] = v;
+	K.vcur[(size_t)b * n + e] = v;
+}
+
+/* end of an Arnoldi step: j += 1; with a graph loop, continue while any
+ * member iterates and j < maxit */
+__global__ void k_loop_ctrl(Krylov K, int maxit, cudaGraphConditionalHandle h, int set_cond)
+{
+	if (threadIdx.x != 0) return;
+	const int j = *K.jcur + 1;
+	*K.jcur = j;
+	*K.loops += 1;
+	bool any = false;
+	for (int b = 0; b < K.batch; b++) any = any || K.active[b];
+	if (set_cond) cudaGraphSetConditional(h, (any && j < maxit) ? 1u : 0u);
 }
 
 /* h_i (i <= j) from partials into H[:, j] */
-__global__ void k_reduce_h(Krylov K, int j, int nblk)
+__global__ void k_reduce_h(Krylov K, int nblk)
 {
 	const int b = blockIdx.x;
 	if (!K.active[b]) return;
+	const int j = *K.jcur;
 	for (int i = 0; i <= j; i++) {
 		const double h = block_sum(K.part + ((size_t)b * (K.restart + 2) + i) * nblk, nblk);
 		if (threadIdx.x == 0) K.H[(size_t)b * (K.restart + 1) * K.restart + (size_t)i * K.restart + j] = h;
 	}
 }
 
-/* w -= sum_{i<=j} h_i v_i; partial ||w||^2 into part slot restart+1 */
-__global__ void __launch_bounds__(RBS) k_cgs_update(Krylov K, int j, int nblk)
+/* w -= sum_{i<=j} h_i v_i; partial ||w||^2 into part slot restart+1; Z_j = zcur */
+__global__ void __launch_bounds__(RBS) k_cgs_update(Krylov K, int nblk)
 {
 	const int b = blockIdx.y;
 	if (!K.active[b]) return;
+	const int j = *K.jcur;
 	const int n = K.n;
 	const size_t vstep = (size_t)K.batch * n;  // V layout [vector][member][n]
 	const double *Vb = K.V + (size_t)b * n;
 	const double *Hb = K.H + (size_t)b * (K.restart + 1) * K.restart;
 	double *wb = K.w + (size_t)b * n;
+	const double *zc = K.zcur + (size_t)b * n;
+	double *zj = K.Z + (size_t)j * vstep + (size_t)b * n;
 	double s = 0;
 	for (int e = blockIdx.x * RBS + threadIdx.x; e < n; e += nblk * RBS) {
+		zj[e] = zc[e];
 		double x = wb[e];
 		for (int i = 0; i <= j; i++) x -= Hb[(size_t)i * K.restart + j] * Vb[(size_t)i * vstep + e];
 		wb[e] = x;
@@ -506,10 +781,11 @@ __global__ void __launch_bounds__(RBS) k_cgs_update(Krylov K, int j, int nblk)
 }
 
 /* Givens rotation of column j, residual estimate, convergence */
-__global__ void k_givens(Krylov K, int j, int nblk, int maxit)
+__global__ void k_givens(Krylov K, int nblk, int maxit)
 {
 	const int b = blockIdx.x;
 	if (!K.active[b]) return;
+	const int j = *K.jcur;
 	const double hn = sqrt(block_sum(K.part + ((size_t)b * (K.restart + 2) + K.restart + 1) * nblk, nblk));
 	if (threadIdx.x != 0) return;
 	const int m = K.restart;
@@ -582,8 +858,8 @@ cudaError_t precond_setup_t(Precond &P, int *err, const int *active, cudaStream_
 			for (int c = 0; c < P.ncolors; c++) {
 				const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 				if (q1 <= q0) continue;
-				k_ilu_parts<R><<<dim3(q1 - q0, B), BS, 0, s>>>(N, q0, P.part_ptr, P.lev_ptr, P.lev_pos, A, P.pos_cell,
-				                                               P.pnbr, P.pnbrpos, F, D, err, active);
+				k_ilu_parts<R><<<dim3(q1 - q0, B), PW, ilu_smem<R>(P.part_cap), s>>>(
+				    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, A, P.pos_cell, P.pnbr, P.pnbrpos, F, D, err, active);
 				(*nk)++;
 			}
 		} else if (P.type == PC_ILU0) {
@@ -619,15 +895,15 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 		for (int c = 0; c < P.ncolors; c++) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			k_fwd_parts<R><<<dim3(q1 - q0, B), BS, 0, s>>>(N, q0, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell,
-			                                               P.pnbrpos, F, D, y, active);
+			k_fwd_parts<R><<<dim3(q1 - q0, B), PW, sweep_smem<R>(P.part_cap), s>>>(
+			    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell, P.pnbrpos, F, D, y, active);
 			(*nk)++;
 		}
 		for (int c = P.ncolors - 1; c >= 0; c--) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			k_bwd_parts<R><<<dim3(q1 - q0, B), BS, 0, s>>>(N, q0, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell,
-			                                               P.pnbr, P.pnbrpos, F, D, y, z, active);
+			k_bwd_parts<R><<<dim3(q1 - q0, B), PW, sweep_smem<R>(P.part_cap), s>>>(
+			    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell, P.pnbr, P.pnbrpos, F, D, y, z, active);
 			(*nk)++;
 		}
 	} else {
@@ -672,6 +948,7 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 		lev_pos = bo.lev_pos;
 		P.nparts = bo.nparts;
 		P.max_width = bo.max_width;
+		for (size_t k = 0; k + 1 < part_ptr.size(); k++) P.part_cap = std::max(P.part_cap, part_ptr[k + 1] - part_ptr[k]);
 	} else {
 		P.ncolors = h.ncolors;
 		P.cptr = h.color_ptr;
@@ -705,6 +982,21 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 		up((void **)&P.part_ptr, part_ptr.data(), sizeof(int) * part_ptr.size());
 		up((void **)&P.lev_ptr, lev_ptr.data(), sizeof(int) * lev_ptr.size());
 		up((void **)&P.lev_pos, lev_pos.data(), sizeof(int) * lev_pos.size());
+	}
+	if (!e && P.ordering == 1) {
+		// shared memory of the part kernels beyond the 48 KB default
+		const int cap = std::max(P.part_cap, 1);
+		if (prec == 4) {
+			e = cudaFuncSetAttribute(k_fwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<float>(cap));
+			if (!e) e = cudaFuncSetAttribute(k_bwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<float>(cap));
+			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<float>(cap));
+			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<float>(cap));
+		} else {
+			e = cudaFuncSetAttribute(k_fwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>(cap));
+			if (!e) e = cudaFuncSetAttribute(k_bwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>(cap));
+			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<double, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<double>(cap));
+			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<double>(cap));
+		}
 	}
 	const size_t w = prec;
 	if (!e && (type == PC_SGS || type == PC_ILU0)) e = cudaMalloc(&P.F, (size_t)batch * 5 * N * 16 * w);
@@ -768,46 +1060,94 @@ cudaError_t krylov_alloc(Krylov &K, int n, int batch, int restart)
 	al((void **)&K.active, sizeof(int) * B);
 	al((void **)&K.iters, sizeof(int) * B);
 	al((void **)&K.kdone, sizeof(int) * B);
+	al((void **)&K.vcur, sizeof(double) * B * n);
+	al((void **)&K.zcur, sizeof(double) * B * n);
+	al((void **)&K.jcur, sizeof(int));
+	al((void **)&K.loops, sizeof(unsigned));
+	if (!e) e = cudaStreamCreateWithFlags(&K.aux, cudaStreamNonBlocking);
 	return e;
 }
 
 void krylov_free(Krylov &K)
 {
-	void *ps[] = {K.V, K.Z, K.w, K.H, K.cs, K.sn, K.g, K.part, K.scal, K.active, K.iters, K.kdone};
+	void *ps[] = {K.V, K.Z, K.w, K.H, K.cs, K.sn, K.g, K.part, K.scal, K.active, K.iters, K.kdone,
+	              K.vcur, K.zcur, K.jcur, K.loops};
 	for (void *p : ps)
 		if (p) cudaFree(p);
+	if (K.aux) cudaStreamDestroy(K.aux);
 	K = Krylov();
 }
 
+/* one Arnoldi step on stream s (preconditioner, operator, classical
+ * Gram-Schmidt, Givens rotation, next basis vector, loop control) */
+static cudaError_t arnoldi_step(Krylov &K, LinOp &op, const Precond &P, int maxit, cudaStream_t s, int *nk,
+                                cudaGraphConditionalHandle h, int set_cond)
+{
+	const int n = K.n, B = K.batch, m = K.restart, nb = K.nblk;
+	const size_t vstep = (size_t)B * n;
+	cudaError_t e;
+	if ((e = precond_apply(P, K.vcur, K.zcur, K.active, s, nk)) != cudaSuccess) return e;
+	if ((e = op.apply(K.zcur, K.w, K.active, s, nk)) != cudaSuccess) return e;
+	k_dot_partial<<<dim3(nb, B, maxit), RBS, 0, s>>>(n, nb, K.V, n, vstep, K.w, n, K.part, 0, m + 2, K.active, K.jcur);
+	k_reduce_h<<<B, 32, 0, s>>>(K, nb);
+	k_cgs_update<<<dim3(nb, B), RBS, 0, s>>>(K, nb);
+	k_givens<<<B, 32, 0, s>>>(K, nb, maxit);
+	k_next_basis<<<dim3((unsigned)((n + 255) / 256), B), 256, 0, s>>>(K);
+	k_loop_ctrl<<<1, 32, 0, s>>>(K, maxit, h, set_cond);
+	*nk += 6;
+	return cudaGetLastError();
+}
+
 cudaError_t fgmres_solve(Krylov &K, LinOp &op, const Precond &P, const double *b, double *x, int maxit, double rtol,
-                         const int *member_active, cudaStream_t s, int *nk)
+                         const int *member_active, cudaStream_t s, int *nk_fixed, int *nk_iter)
 {
 	const int n = K.n, B = K.batch, m = K.restart, nb = K.nblk;
 	if (maxit > m) maxit = m;  // one cycle (the reference configuration: restart = max_it = 30)
-	const size_t vstep = (size_t)B * n;  // V, Z layout [vector][member][n]
-	const dim3 gr(nb, B);
 	const dim3 ge((unsigned)((n + 255) / 256), B);
 	cudaError_t e;
 	// ||b||, x = 0, v0 = b/||b||
-	k_dot_partial<<<dim3(nb, B, 1), RBS, 0, s>>>(n, nb, b, n, 0, b, n, K.part, 0, m + 2, member_active);
+	k_dot_partial<<<dim3(nb, B, 1), RBS, 0, s>>>(n, nb, b, n, 0, b, n, K.part, 0, m + 2, member_active, nullptr);
 	k_gm_init<<<B, 32, 0, s>>>(K, nb, rtol, member_active);
-	k_scale<<<ge, 256, 0, s>>>(n, b, n, K.V, n, K.scal, 3, K.active, 1, x);
-	*nk += 3;
-	for (int j = 0; j < maxit; j++) {
-		double *vj = K.V + (size_t)j * vstep;
-		double *zj = K.Z + (size_t)j * vstep;
-		if ((e = precond_apply(P, vj, zj, K.active, s, nk)) != cudaSuccess) return e;
-		if ((e = op.apply(zj, K.w, K.active, s, nk)) != cudaSuccess) return e;
-		k_dot_partial<<<dim3(nb, B, j + 1), RBS, 0, s>>>(n, nb, K.V, n, vstep, K.w, n, K.part, 0, m + 2, K.active);
-		k_reduce_h<<<B, 32, 0, s>>>(K, j, nb);
-		k_cgs_update<<<gr, RBS, 0, s>>>(K, j, nb);
-		k_givens<<<B, 32, 0, s>>>(K, j, nb, maxit);
-		k_scale<<<ge, 256, 0, s>>>(n, K.w, n, K.V + (size_t)(j + 1) * vstep, n, K.scal, 2, K.active, 0, nullptr);
-		*nk += 5;
+	k_first_basis<<<ge, 256, 0, s>>>(K, b, x);
+	*nk_fixed += 3;
+	cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+	if ((e = cudaStreamIsCapturing(s, &cst)) != cudaSuccess) return e;
+	*nk_iter = 0;
+	if (cst == cudaStreamCaptureStatusActive) {
+		// WHILE node in the graph being captured; its body is one Arnoldi step
+		cudaGraph_t g;
+		const cudaGraphNode_t *deps = nullptr;
+		size_t nd = 0;
+		if ((e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
+		cudaGraphConditionalHandle h;
+		if ((e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+		cudaGraphNodeParams cp = {};
+		cp.type = cudaGraphNodeTypeConditional;
+		cp.conditional.handle = h;
+		cp.conditional.type = cudaGraphCondTypeWhile;
+		cp.conditional.size = 1;
+		cudaGraphNode_t node;
+		if ((e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp)) != cudaSuccess) return e;
+		if ((e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) != cudaSuccess)
+			return e;
+		cudaGraph_t body = cp.conditional.phGraph_out[0];
+		if ((e = cudaStreamBeginCaptureToGraph(K.aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+			return e;
+		cudaError_t e1 = arnoldi_step(K, op, P, maxit, K.aux, nk_iter, h, 1);
+		cudaError_t e2 = cudaStreamEndCapture(K.aux, &body);
+		if (e1 != cudaSuccess) return e1;
+		if (e2 != cudaSuccess) return e2;
+	} else {
+		for (int j = 0; j < maxit; j++) {
+			int nki = 0;
+			if ((e = arnoldi_step(K, op, P, maxit, s, &nki, 0, 0)) != cudaSuccess) return e;
+			*nk_iter = nki;
+			*nk_fixed += nki;
+		}
 	}
 	k_backsolve<<<(B + 31) / 32, 32, 0, s>>>(K, member_active);
 	k_update_x<<<ge, 256, 0, s>>>(K, x, member_active);
-	*nk += 2;
+	*nk_fixed += 2;
 	return cudaGetLastError();
 }
 

@@ -24,6 +24,7 @@ struct Precond {
 	int ordering = 1;           // 0: point colours, 1: block colours (parts of ~part_size cells)
 	int part_size = 128;
 	int nparts = 0, max_width = 0;
+	int part_cap = 0;           // cells in the largest part (shared-memory staging size)
 	std::vector<int> cptr;      // point colours: position range of each colour
 	std::vector<int> cpart;     // block colours: part range of each colour
 	int *part_ptr = nullptr;    // [nparts+1] position range of each part
@@ -40,7 +41,9 @@ struct Precond {
 	BlockMatrix *A = nullptr;   // source matrix (cell order)
 };
 
-/* ordering: 0 point colours, 1 block colours with parts of ~part_size cells */
+/* ordering: 0 point colours, 1 block colours with parts of at most part_size
+ * cells (1 <= part_size <= kMaxPartSize: a part is staged in shared memory) */
+constexpr int kMaxPartSize = 256;
 cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec, int ordering = 1,
                           int part_size = 128);
 void precond_free(Precond &P);
@@ -68,6 +71,11 @@ struct Krylov {
 	int *active = nullptr;      // [batch] member still iterating
 	int *iters = nullptr;       // [batch] iterations done in this solve
 	int *kdone = nullptr;       // [batch] Krylov dimension used
+	double *vcur = nullptr;     // [batch][n] the basis vector being preconditioned (copy of V_j)
+	double *zcur = nullptr;     // [batch][n] its preconditioned image (copied into Z_j)
+	int *jcur = nullptr;        // iteration index j (device; all members share it)
+	unsigned *loops = nullptr;  // Arnoldi iterations executed since the counter was last cleared
+	cudaStream_t aux = nullptr; // stream the loop body is captured on
 };
 
 cudaError_t krylov_alloc(Krylov &K, int n, int batch, int restart);
@@ -81,9 +89,13 @@ struct LinOp {
 
 /* Solves Op x = b to ||b - Op x|| <= rtol ||b|| (or maxit iterations) for
  * every member whose member_active flag is set (NULL = all).  The iteration
- * count per member lands in K.iters.  The sequence of launches does not depend
- * on data, so it can be captured in a CUDA graph. */
+ * count per member lands in K.iters.  The iteration index lives in device
+ * memory, so one Arnoldi step is a fixed launch sequence.  Outside stream
+ * capture the host issues maxit such steps (members that converged skip their
+ * work); under stream capture the step becomes the body of a CUDA-graph WHILE
+ * conditional node that the device stops once no member is iterating.
+ * nk_fixed / nk_iter receive the launches outside / inside one step. */
 cudaError_t fgmres_solve(Krylov &K, LinOp &op, const Precond &P, const double *b, double *x, int maxit, double rtol,
-                         const int *member_active, cudaStream_t s, int *nk);
+                         const int *member_active, cudaStream_t s, int *nk_fixed, int *nk_iter);
 
 }  // namespace fvg

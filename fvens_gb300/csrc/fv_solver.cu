@@ -10,7 +10,9 @@
 // Every step runs on the device without host decisions: CFL ramp, pseudo-time
 // term, relaxation, residual norm, NaN detection and convergence flags are
 // per-member device scalars, so one step is a fixed launch sequence that is
-// captured once in a CUDA graph and replayed; the host only polls the flags
+// captured once in a CUDA graph and replayed; the Krylov iterations inside it
+// are a device-controlled WHILE loop node, so a step runs only as many
+// Arnoldi steps as its slowest member needs.  The host only polls the flags
 // every few steps.  Members of a batch that converged or failed are masked
 // out of every launch.
 #include <algorithm>
@@ -106,6 +108,19 @@ __global__ void __launch_bounds__(RBS) k_update(int N, int nblk, double *__restr
 			const double dl = fmax(dp, dr);
 			om = minf;
 			if (dl < 1.0 - minf) om = 1.0 - dl;
+			// mode 2 (not in the reference): above the threshold the factor
+			// also keeps the relative density / pressure change at minf (1 - minf),
+			// and it is halved until the exact updated density and pressure stay
+			// above minf times their old values
+			else if (nl_update == 2) om = minf * (1.0 - minf) / dl;
+			if (nl_update == 2) {
+				for (int k = 0; k < 40; k++) {
+					const double r1 = uu[0] + om * dd[0], m1 = uu[1] + om * dd[1], m2 = uu[2] + om * dd[2];
+					const double p1 = (g - 1.0) * (uu[3] + om * dd[3] - 0.5 * (m1 * m1 + m2 * m2) / r1);
+					if (r1 >= minf * uu[0] && p1 >= minf * p) break;
+					om *= 0.5;
+				}
+			}
 		}
 		uv.x += om * dv.x; uv.y += om * dv.y; uv.z += om * dv.z; uv.w += om * dv.w;
 		*ub = uv;
@@ -295,7 +310,8 @@ struct fv_solver {
 	cudaGraphExec_t exec = nullptr;
 	cudaGraph_t graph = nullptr;
 	bool graph_ready = false;
-	long long kernels_per_step = 0;
+	long long kernels_per_step = 0;  // launches of one step outside the Arnoldi loop + one Arnoldi step
+	int kernels_fixed = 0, kernels_iter = 0;
 	MatrixOp mop;
 	MatrixFreeOp mfop;
 };
@@ -314,7 +330,9 @@ cudaError_t salloc(fv_solver *S, T **p, size_t n)
 }
 
 /* one pseudo-time step for all active members (fixed launch sequence) */
-cudaError_t solver_step(fv_solver *S, double *u, cudaStream_t s, int *nk)
+/* One pseudo-time step.  nk: launches outside the Arnoldi loop (with the
+ * host-issued loop: all launches); nk_iter: launches of one Arnoldi step. */
+cudaError_t solver_step(fv_solver *S, double *u, cudaStream_t s, int *nk, int *nk_iter)
 {
 	fv_disc_impl *D = S->D;
 	const int N = D->d.nelem, B = D->batch;
@@ -337,7 +355,7 @@ cudaError_t solver_step(fv_solver *S, double *u, cudaStream_t s, int *nk)
 	*nk += 2;
 	if ((e = precond_setup(S->P, S->S.pc_err, S->S.active, s, nk))) return e;
 	LinOp &op = c.matrix_free ? (LinOp &)S->mfop : (LinOp &)S->mop;
-	if ((e = fgmres_solve(S->K, op, S->P, S->r, S->du, c.ksp_maxit, c.ksp_rtol, S->S.active, s, nk))) return e;
+	if ((e = fgmres_solve(S->K, op, S->P, S->r, S->du, c.ksp_maxit, c.ksp_rtol, S->S.active, s, nk, nk_iter))) return e;
 	k_update<<<dim3(S->nblk, B), RBS, 0, s>>>(N, S->nblk, u, S->du, S->r, D->d.area, D->d.phys, c.nl_update,
 	                                           c.min_relax, S->part, S->S);
 	k_norm<<<B, 32, 0, s>>>(B, S->nblk, S->part, S->S, S->K.iters, c.tolerance, c.abs_tolerance, c.max_timesteps);
@@ -351,8 +369,8 @@ extern "C" {
 
 fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, int ordering, int part_size, fv_precond **out)
 {
-	if (!D || !M || !out || M->owner != D || type < FV_PC_NONE || type > FV_PC_ILU0) {
-		set_error("invalid argument");
+	if (!D || !M || !out || M->owner != D || type < FV_PC_NONE || type > FV_PC_ILU0 || part_size > kMaxPartSize) {
+		set_error("invalid argument (part_size at most " + std::to_string(kMaxPartSize) + ")");
 		return FV_ERR_INVALID;
 	}
 	fv_precond *p = new fv_precond();
@@ -436,8 +454,8 @@ fv_status fv_ksp_solve(fv_precond *p, const double *b, double *x, int restart, i
 	MatrixOp op;
 	op.A = &p->M->A;
 	op.cnbr = D->d.cnbr;
-	int nk = 0;
-	e = fgmres_solve(p->K, op, p->P, b, x, maxit, rtol, nullptr, D->stream, &nk);
+	int nk = 0, nki = 0;
+	e = fgmres_solve(p->K, op, p->P, b, x, maxit, rtol, nullptr, D->stream, &nk, &nki);
 	count_launches(nk);
 	if (!e && iters) e = cudaMemcpyAsync(iters, p->K.iters, sizeof(int) * D->batch, cudaMemcpyDeviceToHost, D->stream);
 	if (!e) e = cudaStreamSynchronize(D->stream);
@@ -464,6 +482,14 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	if (D->d.jflux == FV_FLUX_VANLEER || D->d.jflux == FV_FLUX_AUSMPLUS) {
 		set_error("the Jacobian flux has no Jacobian in the reference (VanLeer / AUSM+)");
 		return FV_ERR_UNSUPPORTED;
+	}
+	if (cfg->pc_part_size > kMaxPartSize) {
+		set_error("pc_part_size at most " + std::to_string(kMaxPartSize));
+		return FV_ERR_INVALID;
+	}
+	if (cfg->nl_update < 0 || cfg->nl_update > 2) {
+		set_error("invalid nonlinear update scheme");
+		return FV_ERR_INVALID;
 	}
 	if (cfg->nl_update && (cfg->min_relax <= 0 || cfg->min_relax > 1.0)) {
 		set_error("Minimum relaxation factor is invalid!");
@@ -559,15 +585,18 @@ fv_status fv_solver_solve(fv_solver *S, double *u, const int *member_mask, fv_so
 		if (S->graph) { cudaGraphDestroy(S->graph); S->graph = nullptr; }
 		e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
 		if (!e) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-		int nk = 0;
+		int nk = 0, nki = 0;
 		if (!e) {
-			cudaError_t e1 = solver_step(S, u, cs, &nk);
+			cudaError_t e1 = solver_step(S, u, cs, &nk, &nki);
 			cudaError_t e2 = cudaStreamEndCapture(cs, &S->graph);
 			e = e1 ? e1 : e2;
 		}
 		if (!e) e = cudaGraphInstantiate(&S->exec, S->graph, 0);
-		S->kernels_per_step = nk;
+		S->kernels_fixed = nk;
+		S->kernels_iter = nki;
+		S->kernels_per_step = nk + nki;
 	}
+	if (!e) e = cudaMemsetAsync(S->K.loops, 0, sizeof(unsigned), s);
 	std::vector<int> act(B), status(B, 0);
 	int steps_launched = 0;
 	const int maxit = S->cfg.max_timesteps;
@@ -576,10 +605,10 @@ fv_status fv_solver_solve(fv_solver *S, double *u, const int *member_mask, fv_so
 		for (int k = 0; k < chunk && !e; k++) {
 			if (graph) {
 				e = cudaGraphLaunch(S->exec, s);
-				count_launches(S->kernels_per_step);
+				count_launches(S->kernels_fixed);
 			} else {
-				int nk = 0;
-				e = solver_step(S, u, s, &nk);
+				int nk = 0, nki = 0;
+				e = solver_step(S, u, s, &nk, &nki);
 				count_launches(nk);
 				S->kernels_per_step = nk;
 			}
@@ -594,6 +623,12 @@ fv_status fv_solver_solve(fv_solver *S, double *u, const int *member_mask, fv_so
 	}
 	if (cs) cudaStreamDestroy(cs);
 	if (dmask) cudaFree(dmask);
+	if (!e && graph) {
+		// Arnoldi steps the graph's loop node executed
+		unsigned loops = 0;
+		e = cudaMemcpy(&loops, S->K.loops, sizeof(unsigned), cudaMemcpyDeviceToHost);
+		count_launches((long long)loops * S->kernels_iter);
+	}
 	if (e) return cuda_status(e, "steady solve");
 	// statistics
 	std::vector<double> res(B), res0(B), cfl(B);

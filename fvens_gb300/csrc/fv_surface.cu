@@ -1,0 +1,108 @@
+/*
+ * Wall surface functionals: lift, pressure drag and skin-friction drag
+ * coefficients over the faces of one boundary marker, FP64, for every member
+ * of the batch (FlowFV_base::computeSurfaceData, flow_spatial.cpp:130-310 of
+ * the reference; the per-face Cp and Cf output arrays are not produced).
+ *
+ * Per wall face f with unit normal n, length len, tangent t = (n_y, -n_x),
+ * cell-centred conserved state u of its interior cell and that cell's
+ * conserved gradients (getGradients, flow_spatial.cpp:95-112):
+ *   Cp   = 2 (p(u) - p_inf)
+ *   Cf   = 2 mu(T(u)) ((grad v + grad v^T) n) . t,
+ *          grad v_ij = (d_j(rho v_i) rho - rho v_i d_j rho) / rho^2
+ *   Cl   = sum Cp (n . w_perp) len / sum len,   w = (cos aoa, sin aoa),
+ *   CDp  = sum Cp (n . w) len / sum len,        w_perp = (-w_y, w_x)
+ *   CDsf = sum Cf (t . w) len / sum len
+ * The sums are a fixed-order tree reduction (one CTA per member), so results
+ * are bitwise reproducible.
+ */
+#include <cuda_runtime.h>
+
+#include "fv_abi_internal.hpp"
+
+namespace fvg {
+namespace {
+
+constexpr int SBS = 256;
+
+__global__ void __launch_bounds__(SBS) k_surface(DiscDev D, const double *__restrict__ u, const d4 *__restrict__ grad,
+                                                  const int *__restrict__ btag, int marker, double *__restrict__ out)
+{
+	const int b = blockIdx.x;
+	const Phys P = D.phys[b];
+	const double wx = cos(P.aoa), wy = sin(P.aoa);
+	const double fnx = -wy, fny = wx;
+	const size_t N = D.nelem;
+	double acc[4] = {0, 0, 0, 0};  // Cl, CDp, CDsf, total length
+	for (int f = threadIdx.x; f < D.nbface; f += SBS) {
+		if (btag[f] != marker) continue;
+		const int le = D.flr[f].x;
+		const d4 g4 = D.fgeo[f];
+		const double nx = g4.x, ny = g4.y, len = g4.z;
+		const double tx = ny, ty = -nx;
+		const d4 uc = reinterpret_cast<const d4 *>(u)[(size_t)b * N + le];
+		const double rho = uc.x;
+		const double p = P.gm1 * (uc.w - 0.5 * (uc.y * uc.y + uc.z * uc.z) / rho);
+		const double cp = (p - P.pinf) * 2.0;
+		const double Tt = P.tcoef * p / rho;
+		const double mu = P.sutK / (Tt + P.sutC) * Tt * sqrt(Tt);
+		// conserved gradients, 2x4 column-major: (d_x q0, d_y q0, d_x q1, d_y q1), (d_x q2, d_y q2, ...)
+		const d4 g0 = grad[2 * ((size_t)b * N + le)], g1 = grad[2 * ((size_t)b * N + le) + 1];
+		const double dr[2] = {g0.x, g0.y}, dmu[2] = {g0.z, g0.w}, dmv[2] = {g1.x, g1.y};
+		const double mom[2] = {uc.y, uc.z};
+		const double *dm[2] = {dmu, dmv};
+		double gu[2][2];
+		for (int i = 0; i < 2; i++)
+			for (int j = 0; j < 2; j++) gu[i][j] = (dm[i][j] * rho - mom[i] * dr[j]) / (rho * rho);
+		const double nn[2] = {nx, ny};
+		double force[2];
+		for (int i = 0; i < 2; i++) {
+			force[i] = 0;
+			for (int j = 0; j < 2; j++) force[i] += (gu[i][j] + gu[j][i]) * nn[j];
+		}
+		const double cf = 2.0 * mu * (force[0] * tx + force[1] * ty);
+		acc[0] += cp * (nx * fnx + ny * fny) * len;
+		acc[1] += cp * (nx * wx + ny * wy) * len;
+		acc[2] += cf * (tx * wx + ty * wy) * len;
+		acc[3] += len;
+	}
+	__shared__ double sh[4][SBS];
+	for (int k = 0; k < 4; k++) sh[k][threadIdx.x] = acc[k];
+	__syncthreads();
+	for (int o = SBS / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o)
+			for (int k = 0; k < 4; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x < 4) out[4 * b + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+}  // namespace
+}  // namespace fvg
+
+using namespace fvg;
+
+extern "C" fv_status fv_surface_data(fv_disc *D, const double *u, int marker, double *h_out)
+{
+	if (!D || !u || !h_out) { set_error("null argument"); return FV_ERR_INVALID; }
+	const int B = D->batch;
+	bool found = false;
+	for (int t : D->mesh->h.btag) found = found || t == marker;
+	if (!found) { set_error("no boundary face has marker " + std::to_string(marker)); return FV_ERR_INVALID; }
+	const int before = D->kernels_launched;
+	// conserved gradients into the residual scratch (as FlowFV_base::getGradients)
+	cudaError_t e = gradients_launch(D, u, reinterpret_cast<double *>(D->w.grad), 1, D->stream);
+	if (!e) {
+		k_surface<<<B, SBS, 0, D->stream>>>(D->d, u, D->w.grad, D->btag, marker, D->surf);
+		D->kernels_launched++;
+		e = cudaGetLastError();
+	}
+	count_launches(D->kernels_launched - before);
+	std::vector<double> s(4 * (size_t)B);
+	if (!e) e = cudaMemcpyAsync(s.data(), D->surf, sizeof(double) * 4 * B, cudaMemcpyDeviceToHost, D->stream);
+	if (!e) e = cudaStreamSynchronize(D->stream);
+	if (e) return cuda_status(e, "surface data");
+	for (int b = 0; b < B; b++)
+		for (int k = 0; k < 3; k++) h_out[3 * b + k] = s[4 * b + k] / s[4 * b + 3];
+	return FV_OK;
+}

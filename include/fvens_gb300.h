@@ -152,6 +152,11 @@ fv_status fv_compute_residual(fv_disc *d, const double *d_u, double *d_r, int ge
  * ((x,v0),(y,v0),(x,v1),...).  With primitive != 0: the primitive-variable
  * gradients the second-order residual uses. */
 fv_status fv_get_gradients(fv_disc *d, const double *d_u, double *d_grad, int primitive);
+/* FlowFV_base::computeSurfaceData (flow_spatial.cpp:130-310): lift, pressure
+ * drag and skin-friction drag coefficients over the boundary faces of marker
+ * wall_marker, from the cell-centred state and its conserved gradients, FP64.
+ * h_out[3*batch] = (Cl, CDp, CDsf) per condition (host).  Synchronises. */
+fv_status fv_surface_data(fv_disc *d, const double *d_u, int wall_marker, double *h_out);
 
 /* ---- Jacobian: Spatial::assemble_jacobian (aspatial.cpp:242-340) ---- */
 /* precision 4: FP32 blocks, 8: FP64 blocks */
@@ -201,13 +206,17 @@ typedef struct {
 	double ksp_rtol;
 	int matrix_free;           /* -matrix_free_jacobian */
 	double mf_eps;             /* -matrix_free_difference_step */
-	int nl_update;             /* 0 full, 1 robust_flow (FlowSimpleUpdate) */
+	int nl_update;             /* 0 full, 1 robust_flow (FlowSimpleUpdate), 2 robust_flow whose
+	                              factor above the threshold is min_relax (1 - min_relax) / danger
+	                              and is then halved until the updated density and pressure stay
+	                              above min_relax times their old values (positivity; not in the
+	                              reference) */
 	double min_relax;          /* min_nonlinear_relaxation_factor */
 	int precision;             /* stored Jacobian and preconditioner: 4 FP32, 8 FP64 */
 	int check_every;           /* steps between host polls of the convergence flags */
 	int use_graph;             /* replay each step as a captured CUDA graph */
 	int pc_ordering;           /* 1 block colours (default), 0 point colours */
-	int pc_part_size;          /* cells per part of the block-colour order (default 128) */
+	int pc_part_size;          /* cells per part of the block-colour order (default 128, at most 256) */
 } fv_solver_cfg;
 typedef struct {
 	int steps, lin_iters, status; /* status: FV_OK, FV_ERR_NUMERICAL, FV_ERR_TOLERANCE */

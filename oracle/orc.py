@@ -183,7 +183,7 @@ class Disc:
         u = np.array(u, np.float64, copy=True)
         cd = np.array([cflmin, cflmax, tol, lin_rtol, mf_eps, min_relax])
         ci = np.array([maxiter, int(abs_tol), {"none": 0, "jacobi": 1, "sgs": 2, "ilu0": 3}[pc], restart, lin_maxit,
-                       int(matrix_free), 0 if nl_update == "full" else 1], np.int32)
+                       int(matrix_free), {"full": 0, "robust_flow": 1, "bounded": 2}[nl_update]], np.int32)
         st = np.zeros(6)
         hist = np.zeros((maxiter, 3))
         o = None if order is None else np.ascontiguousarray(order, np.int32)

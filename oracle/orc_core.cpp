@@ -1104,7 +1104,7 @@ struct SolverCfg {
 	double lin_rtol = 0.1;
 	int matrix_free = 0;
 	double mf_eps = 1e-7;
-	int nl_update = 0;      // 0 full, 1 robust_flow (FlowSimpleUpdate)
+	int nl_update = 0;      // 0 full, 1 robust_flow (FlowSimpleUpdate), 2 robust_flow with bounded change
 	double min_relax = 0.2;
 };
 
@@ -1123,7 +1123,7 @@ inline double exp_residual_ramp(double cflmin, double cflmax, double prevcfl, do
 }
 
 /* FlowSimpleUpdate::getLocalRelaxationFactor, nonlinearrelaxation.cpp:25-38 */
-inline double relax_factor(const Phys &P, double minf, const double *du, const double *u)
+inline double relax_factor(const Phys &P, double minf, const double *du, const double *u, int mode)
 {
 	const double p = pressure_from_cons(P, u);
 	const double dp = std::fabs(delta_pressure(P, u, du)) / p;
@@ -1131,6 +1131,20 @@ inline double relax_factor(const Phys &P, double minf, const double *du, const d
 	const double dl = std::max(dp, dr);
 	double om = minf;
 	if (dl < 1.0 - minf) om = 1.0 - dl;
+	// mode 2 (not in the reference): above the threshold the factor also
+	// keeps the relative density / pressure change at minf (1 - minf), and it
+	// is halved until the updated density and pressure (the exact ones, which
+	// the linearised change misses when the momentum changes a lot) stay above
+	// minf times their old values
+	else if (mode == 2) om = minf * (1.0 - minf) / dl;
+	if (mode == 2) {
+		for (int k = 0; k < 40; k++) {
+			double un[4];
+			for (int q = 0; q < 4; q++) un[q] = u[q] + om * du[q];
+			if (un[0] >= minf * u[0] && pressure_from_cons(P, un) >= minf * p) break;
+			om *= 0.5;
+		}
+	}
 	return om;
 }
 
@@ -1183,7 +1197,7 @@ inline int steady_solve(const Disc &D, const SolverCfg &c, double *u, SolveStats
 		}
 		st.lin_iters += its;
 		for (int i = 0; i < ne; i++) {
-			const double om = c.nl_update ? relax_factor(D.P, c.min_relax, &du[4 * i], &u[4 * i]) : 1.0;
+			const double om = c.nl_update ? relax_factor(D.P, c.min_relax, &du[4 * i], &u[4 * i], c.nl_update) : 1.0;
 			for (int q = 0; q < 4; q++) u[4 * i + q] += om * du[4 * i + q];
 		}
 		double rn2 = 0;

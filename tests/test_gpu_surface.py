@@ -1,0 +1,57 @@
+"""Wall surface functionals (Cl, CDp, CDsf) on the GPU against the oracle's
+restatement of FlowFV_base::computeSurfaceData (flow_spatial.cpp:130-310)."""
+import numpy as np
+import pytest
+
+import fvens_gb300 as fv
+from oracle import orc
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+SURFACE_CASES = [
+    ("inviscid_hllc_gg", cases.naca, dict(Minf=0.8, aoa_deg=1.25), dict(flux="HLLC", gradient="GREENGAUSS"),
+     cases.NACA_INV_BCS),
+    ("viscous_wls_sutherland", cases.naca_visc, dict(Minf=0.5, Reinf=5000.0, viscous=True, aoa_deg=2.0),
+     dict(flux="ROE"), cases.NACA_VISC_BCS),
+    ("viscous_first_order", cases.naca_visc, dict(Minf=0.4, Reinf=3000.0, viscous=True, aoa_deg=-3.0),
+     dict(flux="ROE", gradient="NONE"), cases.NACA_VISC_BCS),
+]
+
+
+@pytest.mark.parametrize("name,mesh,phys,num,bcs", SURFACE_CASES, ids=[c[0] for c in SURFACE_CASES])
+def test_surface_data_matches_oracle(cuda, name, mesh, phys, num, bcs):
+    import torch
+    m = mesh()
+    gd = fv.FlowFV(m, fv.physics_cfg(**phys), fv.numerics_cfg(**num), bcs)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), **phys, **num, bcs=bcs)
+    u = cases.perturbed_state(od.freestream(), m.nelem)
+    got = gd.surface_data(torch.tensor(u, device=cuda), 2)[0]
+    ref = od.surface_data(u, 2)
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= 1e-12 * scale, (got, ref)
+    if phys.get("viscous") and num.get("gradient") != "NONE":
+        assert abs(ref[2]) > 0  # skin friction from the conserved gradients
+
+
+def test_surface_data_batch_members_independent(cuda):
+    import torch
+    m = cases.naca_visc()
+    plist = [dict(Minf=0.5, Reinf=5000.0, viscous=True, aoa_deg=1.0),
+             dict(Minf=0.3, Reinf=2000.0, viscous=True, aoa_deg=-2.0)]
+    gd = fv.FlowFV(m, [fv.physics_cfg(**p) for p in plist], fv.numerics_cfg(flux="ROE"), cases.NACA_VISC_BCS)
+    us = [cases.perturbed_state(u, m.nelem, seed=7 + k) for k, u in enumerate(gd.freestream())]
+    got = gd.surface_data(torch.tensor(np.concatenate(us), device=cuda), 2)
+    for k, p in enumerate(plist):
+        od = orc.Disc(orc.Mesh.from_export(m.export()), **p, flux="ROE", bcs=cases.NACA_VISC_BCS)
+        ref = od.surface_data(us[k], 2)
+        assert np.abs(got[k] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_surface_data_unknown_marker_rejected(cuda):
+    import torch
+    m = cases.naca()
+    gd = fv.FlowFV(m, fv.physics_cfg(Minf=0.5), fv.numerics_cfg(flux="ROE"), cases.NACA_INV_BCS)
+    u = torch.tensor(np.tile(gd.freestream()[0], (m.nelem, 1)), device=cuda)
+    with pytest.raises(fv.FvensError):
+        gd.surface_data(u, 99)
