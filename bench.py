@@ -350,6 +350,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain", action="store_true", help="FP64 Jacobian and preconditioner (the plain path)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="profiling aid: issue every launch from the host instead of replaying a CUDA graph")
     ap.add_argument("--max-main-steps", type=int, default=0,
                     help="profiling aid: cap the main solve's pseudo-time steps (the solve then does not converge)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -362,6 +364,9 @@ def main():
     args = ap.parse_args()
     if args.max_main_steps > 0:
         MAIN["max_timesteps"] = args.max_main_steps
+    if args.no_graph:
+        STARTER["use_graph"] = 0
+        MAIN["use_graph"] = 0
     if args.impl == "reference":
         run_reference(args)
     else:
