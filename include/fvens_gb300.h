@@ -147,6 +147,15 @@ fv_status fv_disc_freestream(const fv_disc *d, double *h_uinf);
 /* Spatial::compute_residual (aspatial.hpp:64): d_r += -R(d_u); when
  * gettimesteps, d_dt[nelem*batch] receives the local time steps. */
 fv_status fv_compute_residual(fv_disc *d, const double *d_u, double *d_r, int gettimesteps, double *d_dt);
+/* fv_compute_residual with its scratch in one static device array of the
+ * library (64 MiB) instead of the handle's own buffers; no counterpart in the
+ * reference.  For callers whose evaluation path must not allocate device
+ * memory: neither the call nor its set-up allocates.  The first call on a
+ * device (that device current) looks up the array's address -- make it
+ * before any stream capture.  Discretisations whose scratch (cells x batch)
+ * exceeds the array are rejected with FV_ERR_INVALID.  All calls share the
+ * array: calls whose GPU work overlaps race on it. */
+fv_status fv_compute_residual_static(fv_disc *d, const double *d_u, double *d_r, int gettimesteps, double *d_dt);
 /* FlowFV_base::getGradients (flow_spatial.cpp:95-112): conserved-variable
  * cell gradients, nelem x 8 per condition in GradBlock_t order
  * ((x,v0),(y,v0),(x,v1),...).  With primitive != 0: the primitive-variable
