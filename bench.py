@@ -133,7 +133,11 @@ def run_ours(args):
     def solve_device():
         ud.copy_(u0d)
         _, st1 = S1.solve(ud, raise_on_error=False)
+        if args.nvtx:
+            torch.cuda.nvtx.range_push("main_solve")
         rc, st2 = S2.solve(ud, raise_on_error=False)
+        if args.nvtx:
+            torch.cuda.nvtx.range_pop()
         return st1[0], st2[0]
 
     def barrier():
@@ -350,6 +354,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain", action="store_true", help="FP64 Jacobian and preconditioner (the plain path)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nvtx", action="store_true", help="profiling aid: NVTX range around each main solve")
     ap.add_argument("--no-graph", action="store_true",
                     help="profiling aid: issue every launch from the host instead of replaying a CUDA graph")
     ap.add_argument("--max-main-steps", type=int, default=0,

@@ -225,6 +225,28 @@ class FlowFV:
     def assemble_jacobian(self, u, matrix):
         check(lib().fv_assemble_jacobian(self._h, _vp(dptr(u)), matrix._h))
 
+    def steady_fe_solve(self, u, cfl, tolerance=1e-10, max_timesteps=1000, abs_tolerance=True, raise_on_error=True):
+        """SteadyForwardEulerSolver::solve on the device state u (in place);
+        returns (status, per-member stats)."""
+        c = solver_cfg(cfl_min=cfl, cfl_max=cfl, tolerance=tolerance, max_timesteps=max_timesteps,
+                       abs_tolerance=int(bool(abs_tolerance)))
+        st = (fv_solve_stats * self.batch)()
+        rc = lib().fv_steady_fe_solve(self._h, ctypes.byref(c), _vp(dptr(u)), st)
+        if raise_on_error:
+            check(rc)
+        return rc, [dict(steps=s.steps, status=s.status, res0=s.res0, res=s.res) for s in st]
+
+    def tvdrk_solve(self, u, order, cfl, final_time, max_steps=1000000, raise_on_error=True):
+        """TVDRKSolver::solve on the device state u (in place); returns
+        (status, steps[batch], time[batch])."""
+        steps = np.zeros(self.batch, np.int32)
+        tm = np.zeros(self.batch)
+        rc = lib().fv_tvdrk_solve(self._h, int(order), ctypes.c_double(cfl), ctypes.c_double(final_time),
+                                  int(max_steps), _vp(dptr(u)), _hp(steps, ctypes.c_int), _hp(tm, ctypes.c_double))
+        if raise_on_error:
+            check(rc)
+        return rc, steps, tm
+
     def surface_data(self, u, wall_marker):
         """(Cl, CDp, CDsf) over the faces of wall_marker, one row per batch member
         (FlowFV_base::computeSurfaceData)."""

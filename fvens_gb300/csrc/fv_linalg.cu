@@ -289,17 +289,19 @@ __global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, 
 	bwd_row<R>(nelem, p, b, sgs, pos_cell, pnbr, pnbrpos, F, Dinv, y, z);
 }
 
-/* ---- block-colour sweeps: one warp per part, the part staged in shared memory ----
+/* ---- block-colour sweeps and factorisation: one CTA per part, the part staged in shared memory ----
  *
  * A part's cells occupy the contiguous elimination positions [p0, p1), sorted
- * by dependency level.  Phase 1 (all lanes, coalesced) folds the contributions
- * of neighbours outside the part -- finished by earlier colour launches -- into
- * a right-hand side and copies the blocks that couple the part to itself into
- * shared memory; phase 2 walks the levels with four lanes per cell (one block
- * row each) reading shared memory only; phase 3 writes the part back.  The
- * dependency chain of a part therefore costs shared-memory latency per level,
- * not global-memory latency. */
-constexpr int PW = 32;  // lanes per part CTA: 8 cells x 4 block rows per pass
+ * by dependency level.  Every neighbour of a part cell outside the part lies
+ * in another colour, so it is either finished by an earlier launch (it comes
+ * before the whole part) or untouched until a later one.  Phase 1 (all PT
+ * threads, one cell each) therefore does all the work that involves
+ * neighbours outside the part -- in parallel, with the part's own blocks
+ * copied to shared memory; phase 2 (warp 0, four lanes per cell, one block
+ * row each) walks the part's dependency levels reading shared memory only;
+ * phase 3 (all threads) writes the part back.  The dependency chain of a part
+ * thus costs shared-memory latency per level. */
+constexpr int PT = 128;  // threads per part CTA; warp 0 walks the levels (8 cells x 4 block rows per pass)
 
 /* dynamic shared memory of the sweep kernels for parts of at most cap cells */
 template <class R>
@@ -314,7 +316,7 @@ __device__ __forceinline__ R dot4(const R *a, const R *v) { return a[0] * v[0] +
 /* forward sweep of the parts of one colour: y_p = r_i - sum_{lower} L y (ILU)
  * or Dinv (r_i - sum_{lower} A y) (SGS) */
 template <class R>
-__global__ void __launch_bounds__(PW) k_fwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+__global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const double *__restrict__ r, const int *__restrict__ pos_cell,
                                                   const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
@@ -334,8 +336,7 @@ __global__ void __launch_bounds__(PW) k_fwd_parts(int nelem, int part0, int cap,
 	const R *Fb = F + (size_t)b * 5 * N * 16;
 	R *yb = y + (size_t)b * N * 4;
 	const double4 *rb = reinterpret_cast<const double4 *>(r + (size_t)b * N * 4);
-	const int lane = threadIdx.x;
-	for (int c = lane; c < n; c += PW) {
+	for (int c = threadIdx.x; c < n; c += PT) {
 		const int p = p0 + c;
 		const double4 rv = rb[pos_cell[p]];
 		R s[4] = {R(rv.x), R(rv.y), R(rv.z), R(rv.w)};
@@ -366,38 +367,42 @@ __global__ void __launch_bounds__(PW) k_fwd_parts(int nelem, int part0, int cap,
 			store_blk(sD + (size_t)c * 16, d);
 		}
 	}
-	__syncwarp();
-	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-	const int g = lane >> 2, row = lane & 3;
-	for (int l = l0; l < l1; l++) {
-		const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
-		for (int c0 = ls; c0 < le; c0 += PW / 4) {
-			const int c = c0 + g;
-			const bool on = c < le;
-			R acc = R(0);
-			if (on) {
-				acc = st[4 * c + row];
-				const int4 nb = snb[c];
-				const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
-				for (int j = 0; j < 4; j++)
-					if (l4[j] >= 0) acc -= dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		const int lane = threadIdx.x;
+		const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+		const int g = lane >> 2, row = lane & 3;
+		for (int l = l0; l < l1; l++) {
+			const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
+			for (int c0 = ls; c0 < le; c0 += 8) {
+				const int c = c0 + g;
+				const bool on = c < le;
+				R acc = R(0);
+				if (on) {
+					acc = st[4 * c + row];
+					const int4 nb = snb[c];
+					const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
+					for (int j = 0; j < 4; j++)
+						if (l4[j] >= 0) acc -= dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+				}
+				if (sgs) {
+					if (on) st[4 * c + row] = acc;
+					__syncwarp();
+					if (on) acc = dot4(sD + (size_t)c * 16 + 4 * row, st + 4 * c);
+				}
+				if (on) sv[4 * c + row] = acc;
 			}
-			if (sgs) {
-				if (on) st[4 * c + row] = acc;
-				__syncwarp();
-				if (on) acc = dot4(sD + (size_t)c * 16 + 4 * row, st + 4 * c);
-			}
-			if (on) sv[4 * c + row] = acc;
+			__syncwarp();
 		}
-		__syncwarp();
 	}
-	for (int e = lane; e < 4 * n; e += PW) yb[(size_t)p0 * 4 + e] = sv[e];
+	__syncthreads();
+	for (int e = threadIdx.x; e < 4 * n; e += PT) yb[(size_t)p0 * 4 + e] = sv[e];
 }
 
 /* backward sweep of the parts of one colour (levels in reverse):
  * z_i = Dinv (y_p - sum_{upper} U z) (ILU) or y_p - Dinv sum_{upper} A z (SGS) */
 template <class R>
-__global__ void __launch_bounds__(PW) k_bwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+__global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
                                                   const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
@@ -418,8 +423,7 @@ __global__ void __launch_bounds__(PW) k_bwd_parts(int nelem, int part0, int cap,
 	const R *Fb = F + (size_t)b * 5 * N * 16;
 	const R *yb = y + (size_t)b * N * 4;
 	double *zb = z + (size_t)b * N * 4;
-	const int lane = threadIdx.x;
-	for (int c = lane; c < n; c += PW) {
+	for (int c = threadIdx.x; c < n; c += PT) {
 		const int p = p0 + c;
 		const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
 		const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
@@ -452,43 +456,71 @@ __global__ void __launch_bounds__(PW) k_bwd_parts(int nelem, int part0, int cap,
 		load_blk(Dinv + ((size_t)b * N + p) * 16, d);
 		store_blk(sD + (size_t)c * 16, d);
 	}
-	__syncwarp();
-	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-	const int g = lane >> 2, row = lane & 3;
-	for (int l = l1 - 1; l >= l0; l--) {
-		const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
-		for (int c0 = ls; c0 < le; c0 += PW / 4) {
-			const int c = c0 + g;
-			const bool on = c < le;
-			R acc = R(0);
-			if (on) {
-				const int4 nb = snb[c];
-				const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
-				for (int j = 0; j < 4; j++)
-					if (l4[j] >= 0) acc += dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
-				// ILU: t = (y - outside) - inside;  SGS: t = outside + inside
-				acc = sgs ? st[4 * c + row] + acc : st[4 * c + row] - acc;
-				st[4 * c + row] = acc;
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		const int lane = threadIdx.x;
+		const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+		const int g = lane >> 2, row = lane & 3;
+		for (int l = l1 - 1; l >= l0; l--) {
+			const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
+			for (int c0 = ls; c0 < le; c0 += 8) {
+				const int c = c0 + g;
+				const bool on = c < le;
+				if (on) {
+					const int4 nb = snb[c];
+					const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
+					R acc = R(0);
+					for (int j = 0; j < 4; j++)
+						if (l4[j] >= 0) acc += dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+					// ILU: t = (y - outside) - inside;  SGS: t = outside + inside
+					st[4 * c + row] = sgs ? st[4 * c + row] + acc : st[4 * c + row] - acc;
+				}
+				__syncwarp();
+				if (on) {
+					const R dz = dot4(sD + (size_t)c * 16 + 4 * row, st + 4 * c);
+					sv[4 * c + row] = sgs ? sv[4 * c + row] - dz : dz;
+				}
 			}
 			__syncwarp();
-			if (on) {
-				const R dz = dot4(sD + (size_t)c * 16 + 4 * row, st + 4 * c);
-				sv[4 * c + row] = sgs ? sv[4 * c + row] - dz : dz;
-			}
 		}
-		__syncwarp();
 	}
-	for (int c = lane; c < n; c += PW) {
+	__syncthreads();
+	for (int c = threadIdx.x; c < n; c += PT) {
 		const R *v = sv + 4 * c;
 		reinterpret_cast<double4 *>(zb)[pos_cell[p0 + c]] = make_double4(double(v[0]), double(v[1]), double(v[2]), double(v[3]));
 	}
 }
 
-/* block ILU(0) of the parts of one colour, rows staged in shared memory:
- * row p (IKJ, no fill) is final once every lower neighbour's row is; four
- * lanes per row, lane q owning block row q of every block of the row. */
+/* row i -= its elimination by lower neighbour k (IKJ, no fill): L_ik = A_ik Dinv_k
+ * replaces A_ik, and every column j of row i after k (diagonal and neighbours
+ * at positions > p_k) that row k also holds loses L_ik U_kj.  rw: row i's five
+ * blocks (slot 0 diagonal, 1+j neighbour j); dk, uk: row k's inverted
+ * diagonal and its blocks (slot 1+t for k's neighbour t); kn: k's neighbours. */
+template <class R>
+__device__ __forceinline__ void ilu_eliminate_row(R *rw, int jk, int pk, int icell, const int *nbc, const int *nbp,
+                                                  int p, const R *dk, const R *uk, size_t ustride, const int *kn)
+{
+	R L[16];
+	mm(rw + (1 + jk) * 16, dk, L);
+	for (int q = 0; q < 16; q++) rw[(1 + jk) * 16 + q] = L[q];
+	for (int s = 0; s < 5; s++) {
+		const int colcell = s == 0 ? icell : nbc[s - 1];
+		const int colpos = s == 0 ? p : nbp[s - 1];
+		if (colpos < 0 || colpos <= pk) continue;
+		int ks = -1;
+		for (int t = 0; t < 4; t++)
+			if (kn[t] == colcell) ks = t;
+		if (ks < 0) continue;
+		R ukj[16], prod[16];
+		load_blk(uk + (size_t)(1 + ks) * ustride, ukj);
+		mm(L, ukj, prod);
+		for (int q = 0; q < 16; q++) rw[s * 16 + q] -= prod[q];
+	}
+}
+
+/* block ILU(0) of the parts of one colour */
 template <class R, class RA>
-__global__ void __launch_bounds__(PW) k_ilu_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+__global__ void __launch_bounds__(PT) k_ilu_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   const RA *__restrict__ A, const int *__restrict__ pos_cell,
                                                   const int4 *__restrict__ pnbr, const int4 *__restrict__ pnbrpos,
@@ -505,8 +537,7 @@ __global__ void __launch_bounds__(PW) k_ilu_parts(int nelem, int part0, int cap,
 	const RA *Ab = A + (size_t)b * 5 * N * 16;
 	R *Fb = F + (size_t)b * 5 * N * 16;
 	R *Db = Dinv + (size_t)b * N * 16;
-	const int lane = threadIdx.x;
-	for (int e = lane; e < n * 5; e += PW) {
+	for (int e = threadIdx.x; e < n * 5; e += PT) {
 		const int s = e / n, c = e - s * n;
 		RA tmp[16];
 		R blk[16];
@@ -514,77 +545,96 @@ __global__ void __launch_bounds__(PW) k_ilu_parts(int nelem, int part0, int cap,
 		for (int q = 0; q < 16; q++) blk[q] = R(tmp[q]);
 		store_blk(sRow + ((size_t)c * 5 + s) * 16, blk);
 	}
-	__syncwarp();
-	const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-	const int g = lane >> 2, row = lane & 3;
-	for (int l = l0; l < l1; l++) {
-		const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
-		for (int c0 = ls; c0 < le; c0 += PW / 4) {
-			const int c = c0 + g;
-			const bool on = c < le;
-			if (on) {
-				const int p = p0 + c;
-				const int icell = pos_cell[p];
-				R *rw = sRow + (size_t)c * 80;
-				const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
-				const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
-				const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
-				int ord[4], nl = 0;
-				for (int j = 0; j < 4; j++)
-					if (nbp[j] >= 0 && nbp[j] < p) ord[nl++] = j;
-				for (int a = 1; a < nl; a++)
-					for (int d = a; d > 0 && nbp[ord[d]] < nbp[ord[d - 1]]; d--) { const int t = ord[d]; ord[d] = ord[d - 1]; ord[d - 1] = t; }
-				for (int a = 0; a < nl; a++) {
-					const int jk = ord[a], pk = nbp[jk];
-					const bool inpart = pk >= p0;
-					const R *dk;  // inverted diagonal of row k
-					R dkg[16];
-					if (inpart) dk = sD + (size_t)(pk - p0) * 16;
-					else { load_blk(Db + (size_t)pk * 16, dkg); dk = dkg; }
-					// L_ik = A_ik Dinv_k : lane row computes block row `row`
-					R Lr[4];
-					R *aik = rw + (1 + jk) * 16 + 4 * row;
-					for (int m = 0; m < 4; m++) Lr[m] = aik[0] * dk[m] + aik[1] * dk[4 + m] + aik[2] * dk[8 + m] + aik[3] * dk[12 + m];
-					for (int m = 0; m < 4; m++) aik[m] = Lr[m];
-					const int4 kn4 = pnbr[pk];
-					const int kn[4] = {kn4.x, kn4.y, kn4.z, kn4.w};
-					for (int s = 0; s < 5; s++) {
-						const int colcell = s == 0 ? icell : nbc[s - 1];
-						const int colpos = s == 0 ? p : nbp[s - 1];
-						if (colpos < 0 || colpos <= pk) continue;
-						int ks = -1;
-						for (int t = 0; t < 4; t++)
-							if (kn[t] == colcell) ks = t;
-						if (ks < 0) continue;
-						const R *ukj;
-						R ug[16];
-						if (inpart) ukj = sRow + ((size_t)(pk - p0) * 5 + 1 + ks) * 16;
-						else { load_blk(Fb + ((size_t)(1 + ks) * N + pk) * 16, ug); ukj = ug; }
-						R *ais = rw + s * 16 + 4 * row;
-						for (int m = 0; m < 4; m++) ais[m] -= Lr[0] * ukj[m] + Lr[1] * ukj[4 + m] + Lr[2] * ukj[8 + m] + Lr[3] * ukj[12 + m];
-					}
-				}
-			}
-			__syncwarp();
-			if (on) {
-				R dblk[16], inv[16];
-				for (int q = 0; q < 16; q++) dblk[q] = sRow[(size_t)c * 80 + q];
-				if (!inv4(dblk, inv)) {
-					if (row == 0) atomicOr(err, 1);
-					for (int q = 0; q < 16; q++) inv[q] = R(0);
-				}
-				for (int m = 0; m < 4; m++) sD[(size_t)c * 16 + 4 * row + m] = inv[4 * row + m];
-			}
-			__syncwarp();
+	__syncthreads();
+	// lower neighbours outside the part are final and precede every part cell
+	for (int c = threadIdx.x; c < n; c += PT) {
+		const int p = p0 + c;
+		const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
+		const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+		int ord[4], nl = 0;
+		for (int j = 0; j < 4; j++)
+			if (nbp[j] >= 0 && nbp[j] < p0) ord[nl++] = j;
+		for (int a = 1; a < nl; a++)
+			for (int d = a; d > 0 && nbp[ord[d]] < nbp[ord[d - 1]]; d--) { const int t = ord[d]; ord[d] = ord[d - 1]; ord[d - 1] = t; }
+		for (int a = 0; a < nl; a++) {
+			const int jk = ord[a], pk = nbp[jk];
+			R dk[16];
+			load_blk(Db + (size_t)pk * 16, dk);
+			const int4 kn4 = pnbr[pk];
+			const int kn[4] = {kn4.x, kn4.y, kn4.z, kn4.w};
+			ilu_eliminate_row(sRow + (size_t)c * 80, jk, pk, pos_cell[p], nbc, nbp, p, dk, Fb + (size_t)pk * 16,
+			                  N * 16, kn);
 		}
 	}
-	for (int e = lane; e < n * 5; e += PW) {
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		const int lane = threadIdx.x;
+		const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
+		const int g = lane >> 2, row = lane & 3;
+		for (int l = l0; l < l1; l++) {
+			const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
+			for (int c0 = ls; c0 < le; c0 += 8) {
+				const int c = c0 + g;
+				const bool on = c < le;
+				if (on) {
+					const int p = p0 + c;
+					const int icell = pos_cell[p];
+					R *rw = sRow + (size_t)c * 80;
+					const int4 nb4 = pnbr[p], np4 = pnbrpos[p];
+					const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
+					const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
+					int ord[4], nl = 0;
+					for (int j = 0; j < 4; j++)
+						if (nbp[j] >= p0 && nbp[j] < p) ord[nl++] = j;
+					for (int a = 1; a < nl; a++)
+						for (int d = a; d > 0 && nbp[ord[d]] < nbp[ord[d - 1]]; d--) { const int t = ord[d]; ord[d] = ord[d - 1]; ord[d - 1] = t; }
+					for (int a = 0; a < nl; a++) {
+						const int jk = ord[a], pk = nbp[jk];
+						const R *dk = sD + (size_t)(pk - p0) * 16;
+						// L_ik = A_ik Dinv_k : lane `row` computes block row `row`
+						R Lr[4];
+						R *aik = rw + (1 + jk) * 16 + 4 * row;
+						for (int m = 0; m < 4; m++) Lr[m] = aik[0] * dk[m] + aik[1] * dk[4 + m] + aik[2] * dk[8 + m] + aik[3] * dk[12 + m];
+						for (int m = 0; m < 4; m++) aik[m] = Lr[m];
+						const int4 kn4 = pnbr[pk];
+						const int kn[4] = {kn4.x, kn4.y, kn4.z, kn4.w};
+						for (int s = 0; s < 5; s++) {
+							const int colcell = s == 0 ? icell : nbc[s - 1];
+							const int colpos = s == 0 ? p : nbp[s - 1];
+							if (colpos < 0 || colpos <= pk) continue;
+							int ks = -1;
+							for (int t = 0; t < 4; t++)
+								if (kn[t] == colcell) ks = t;
+							if (ks < 0) continue;
+							const R *ukj = sRow + ((size_t)(pk - p0) * 5 + 1 + ks) * 16;
+							R *ais = rw + s * 16 + 4 * row;
+							for (int m = 0; m < 4; m++) ais[m] -= Lr[0] * ukj[m] + Lr[1] * ukj[4 + m] + Lr[2] * ukj[8 + m] + Lr[3] * ukj[12 + m];
+						}
+					}
+				}
+				__syncwarp();
+				if (on) {
+					R dblk[16], inv[16];
+					for (int q = 0; q < 16; q++) dblk[q] = sRow[(size_t)c * 80 + q];
+					if (!inv4(dblk, inv)) {
+						if (row == 0) atomicOr(err, 1);
+						for (int q = 0; q < 16; q++) inv[q] = R(0);
+					}
+					for (int m = 0; m < 4; m++) sD[(size_t)c * 16 + 4 * row + m] = inv[4 * row + m];
+				}
+				__syncwarp();
+			}
+		}
+	}
+	__syncthreads();
+	for (int e = threadIdx.x; e < n * 5; e += PT) {
 		const int s = e / n, c = e - s * n;
 		R blk[16];
 		for (int q = 0; q < 16; q++) blk[q] = sRow[((size_t)c * 5 + s) * 16 + q];
 		store_blk(Fb + ((size_t)s * N + p0 + c) * 16, blk);
 	}
-	for (int e = lane; e < n; e += PW) {
+	for (int e = threadIdx.x; e < n; e += PT) {
 		R blk[16];
 		for (int q = 0; q < 16; q++) blk[q] = sD[(size_t)e * 16 + q];
 		store_blk(Db + ((size_t)p0 + e) * 16, blk);
@@ -858,7 +908,7 @@ cudaError_t precond_setup_t(Precond &P, int *err, const int *active, cudaStream_
 			for (int c = 0; c < P.ncolors; c++) {
 				const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 				if (q1 <= q0) continue;
-				k_ilu_parts<R><<<dim3(q1 - q0, B), PW, ilu_smem<R>(P.part_cap), s>>>(
+				k_ilu_parts<R><<<dim3(q1 - q0, B), PT, ilu_smem<R>(P.part_cap), s>>>(
 				    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, A, P.pos_cell, P.pnbr, P.pnbrpos, F, D, err, active);
 				(*nk)++;
 			}
@@ -895,14 +945,14 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 		for (int c = 0; c < P.ncolors; c++) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			k_fwd_parts<R><<<dim3(q1 - q0, B), PW, sweep_smem<R>(P.part_cap), s>>>(
+			k_fwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap), s>>>(
 			    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell, P.pnbrpos, F, D, y, active);
 			(*nk)++;
 		}
 		for (int c = P.ncolors - 1; c >= 0; c--) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			k_bwd_parts<R><<<dim3(q1 - q0, B), PW, sweep_smem<R>(P.part_cap), s>>>(
+			k_bwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap), s>>>(
 			    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell, P.pnbr, P.pnbrpos, F, D, y, z, active);
 			(*nk)++;
 		}
@@ -1041,7 +1091,7 @@ cudaError_t krylov_alloc(Krylov &K, int n, int batch, int restart)
 	K.n = n;
 	K.batch = batch;
 	K.restart = restart;
-	K.nblk = std::max(1, std::min(128, (n + RBS * 8 - 1) / (RBS * 8)));
+	K.nblk = std::max(1, std::min(1024, (n + RBS * 4 - 1) / (RBS * 4)));
 	const size_t B = batch;
 	cudaError_t e = cudaSuccess;
 	auto al = [&](void **p, size_t bytes) {

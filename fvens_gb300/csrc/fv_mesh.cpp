@@ -578,49 +578,38 @@ int read_gmsh2(const std::string &path, RawMesh &out, std::string *err)
 
 namespace fvg {
 
-namespace {
-void rcb_split(const std::vector<double> &cc, std::vector<int> &idx, size_t lo, size_t hi, size_t target,
-               std::vector<std::pair<size_t, size_t>> &parts)
-{
-	if (hi - lo <= target) {
-		parts.push_back({lo, hi});
-		return;
-	}
-	double mn[2] = {1e300, 1e300}, mx[2] = {-1e300, -1e300};
-	for (size_t k = lo; k < hi; k++)
-		for (int d = 0; d < 2; d++) {
-			mn[d] = std::min(mn[d], cc[2 * idx[k] + d]);
-			mx[d] = std::max(mx[d], cc[2 * idx[k] + d]);
-		}
-	const int d = (mx[0] - mn[0]) >= (mx[1] - mn[1]) ? 0 : 1;
-	std::stable_sort(idx.begin() + lo, idx.begin() + hi, [&](int a, int b) {
-		const double xa = cc[2 * a + d], xb = cc[2 * b + d];
-		return xa < xb || (xa == xb && a < b);
-	});
-	const size_t mid = lo + (hi - lo) / 2;
-	rcb_split(cc, idx, lo, mid, target, parts);
-	rcb_split(cc, idx, mid, hi, target, parts);
-}
-}  // namespace
-
 BlockOrder block_colour_order(const HostMesh &h, int part_size)
 {
 	BlockOrder o;
 	const int n = h.nelem;
-	std::vector<int> idx(n);
-	std::iota(idx.begin(), idx.end(), 0);
-	std::vector<std::pair<size_t, size_t>> ranges;
-	rcb_split(h.cc, idx, 0, n, std::max(part_size, 1), ranges);
-	const int np = (int)ranges.size();
-	std::vector<int> pid(n);
-	std::vector<std::vector<int>> cells(np);
-	for (int k = 0; k < np; k++) {
-		for (size_t q = ranges[k].first; q < ranges[k].second; q++) {
-			pid[idx[q]] = k;
-			cells[k].push_back(idx[q]);
+	const size_t target = (size_t)std::max(part_size, 1);
+	// parts grown breadth-first over the cell graph, each from the lowest-numbered
+	// cell not yet in a part: compact in the cell graph, so the dependency chains
+	// inside a part are about as long as the part is wide (in cells)
+	std::vector<int> pid(n, -1);
+	std::vector<std::vector<int>> cells;
+	std::vector<int> queue;
+	queue.reserve(target);
+	for (int seed = 0; seed < n; seed++) {
+		if (pid[seed] >= 0) continue;
+		const int k = (int)cells.size();
+		queue.clear();
+		queue.push_back(seed);
+		pid[seed] = k;
+		for (size_t head = 0; head < queue.size() && queue.size() < target; head++) {
+			const int c = queue[head];
+			for (int j = 0; j < h.nnode[c] && queue.size() < target; j++) {
+				const int nb = h.esuel[4 * c + j];
+				if (nb >= 0 && pid[nb] < 0) {
+					pid[nb] = k;
+					queue.push_back(nb);
+				}
+			}
 		}
-		std::sort(cells[k].begin(), cells[k].end());
+		cells.push_back(queue);
+		std::sort(cells.back().begin(), cells.back().end());
 	}
+	const int np = (int)cells.size();
 	// colour the part adjacency graph greedily
 	std::vector<std::vector<int>> padj(np);
 	for (int f = h.nbface; f < h.naface; f++) {

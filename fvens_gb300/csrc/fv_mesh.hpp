@@ -53,8 +53,8 @@ int mesh_from_arrays(HostMesh &m, int npoin, const double *coords, int nelem, co
                      int nbface, const int *bface, const int *btag, int reorder, std::string *err);
 
 /* Block-colour elimination order for the SGS / ILU(0) preconditioners:
- * cells are split into compact parts of about part_size cells by recursive
- * coordinate bisection of the centroids, parts sharing a face get different
+ * cells are split into parts of at most part_size cells grown breadth-first
+ * over the cell graph (each from the lowest-numbered free cell), parts sharing a face get different
  * colours, and the order is colour-major, then part-major, then inside a part
  * by dependency level (ties by cell index).  Within a part the relative order
  * of any two adjacent cells is their index order, so ILU(0) on this order

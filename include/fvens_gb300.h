@@ -259,6 +259,25 @@ long long fv_solver_kernels_per_step(const fv_solver *s);
 #define FV_KERNEL_PRECOND_SETUP 5   /* factorisation */
 fv_status fv_solver_time_kernel(fv_solver *s, const double *d_u, int which, int reps, double *avg_ms, double *bytes);
 
+/* ---- explicit time stepping ---- */
+/* SteadyForwardEulerSolver::solve (aodesolver.cpp:136-282): d_u (device,
+ * every member) += cfg->cfl_min dt/A r with local time steps dt, until the
+ * energy-residual norm meets cfg->tolerance (relative to the first step's, or
+ * absolute with cfg->abs_tolerance) or cfg->max_timesteps steps ran (then
+ * FV_ERR_TOLERANCE, as the reference's Tolerance_error).  The reference ramps a
+ * CFL it never applies; the update uses the initial CFL.  stats[batch].
+ * Synchronises. */
+fv_status fv_steady_fe_solve(fv_disc *d, const fv_solver_cfg *cfg, double *d_u, fv_solve_stats *stats);
+/* TVDRKSolver::solve (aodesolver.cpp:671-765) of temporal order 1..3 with
+ * physical CFL cfl up to final_time, as the reference has it: every stage
+ * evaluates the residual of the step's starting state; the step is
+ * cfl * min_i dt_i.  max_steps bounds the steps (FV_ERR_TOLERANCE when
+ * reached first; the reference has no bound).  h_steps[batch], h_time[batch]
+ * (host, may be NULL) receive the steps taken and the time reached.
+ * Synchronises. */
+fv_status fv_tvdrk_solve(fv_disc *d, int order, double cfl, double final_time, int max_steps, double *d_u,
+                         int *h_steps, double *h_time);
+
 /* ---- pointwise device evaluations (for validation against the reference) ---- */
 /* n states: d_ul, d_ur n x 4, d_n n x 2 -> d_f n x 4 (condition 0's physics) */
 fv_status fv_pointwise_flux(fv_disc *d, int kind, int n, const double *d_ul, const double *d_ur, const double *d_nrm,

@@ -193,6 +193,23 @@ class Disc:
         return u, dict(status=int(status), steps=steps, lin_iters=int(st[1]), res0=st[3], res=st[4], cfl=st[5],
                        history=hist[:steps])
 
+    def steady_fe(self, u, cflinit, tol=1e-10, maxiter=1000, abs_tol=True):
+        """SteadyForwardEulerSolver::solve restated: (u, dict(steps, status, res0, res, history))."""
+        u = np.array(u, np.float64, copy=True)
+        st = np.zeros(4)
+        hist = np.zeros(max(maxiter, 1))
+        lib().orc_steady_fe(self._h, p(np.array([cflinit, tol])), p(np.array([maxiter, int(abs_tol)], np.int32),
+                                                                     ctypes.c_int), p(u), p(st), p(hist))
+        steps = int(st[0])
+        return u, dict(steps=steps, status=int(st[1]), res0=st[2], res=st[3], history=hist[:steps])
+
+    def tvdrk(self, u, order, cfl, final_time):
+        """TVDRKSolver::solve restated: (u, steps, status, time)."""
+        u = np.array(u, np.float64, copy=True)
+        out = np.zeros(3)
+        lib().orc_tvdrk(self._h, int(order), ctypes.c_double(cfl), ctypes.c_double(final_time), p(u), p(out))
+        return u, int(out[0]), int(out[1]), out[2]
+
     def surface_data(self, u, marker):
         out = np.zeros(3)
         lib().orc_surface_data(self._h, p(np.ascontiguousarray(u, np.float64)), int(marker), p(out))

@@ -1422,6 +1422,84 @@ int orc_steady_solve(const void *h, const double *cfg_d, const int *cfg_i, const
 	return e;
 }
 
+/* SteadyForwardEulerSolver::solve, aodesolver.cpp:136-282: u += cflinit dt/A r
+ * with r = -R(u) and dt the local time steps; the ramped CFL the reference
+ * computes is not used by its update.  The loop runs while the (relative, or
+ * here optionally absolute) energy-residual norm exceeds tol; reaching
+ * maxiter is a tolerance failure even on a converged last step, as there.
+ * cfg_d: cflinit, tol; cfg_i: maxiter, abs_tol.  stats_out: steps, status, res0, res */
+int orc_steady_fe(const void *h, const double *cfg_d, const int *cfg_i, double *u, double *stats_out, double *history)
+{
+	const Disc *d = (const Disc *)h;
+	const Mesh &M = *d->m;
+	const int ne = M.nelem;
+	const double cflinit = cfg_d[0], tol = cfg_d[1];
+	const int maxiter = cfg_i[0], abs_tol = cfg_i[1];
+	std::vector<double> r(4 * (size_t)ne), dtm(ne);
+	Disc::Work w;
+	double resi = 1.0, initres = 1.0, res0 = 0;
+	int step = 0, status = 0;
+	while ((abs_tol ? resi > tol : resi / initres > tol) && step < maxiter) {
+		std::fill(r.begin(), r.end(), 0.0);
+		d->residual(u, r.data(), true, dtm.data(), w);
+		for (int i = 0; i < ne; i++)
+			for (int q = 0; q < 4; q++) u[4 * i + q] += cflinit * dtm[i] * 1.0 / M.area[i] * r[4 * i + q];
+		double s = 0;
+		for (int i = 0; i < ne; i++) s += r[4 * i + 3] * r[4 * i + 3] * M.area[i];
+		resi = std::sqrt(s);
+		if (step == 0) { initres = resi; res0 = resi; }
+		if (history) history[step] = resi;
+		step++;
+		if (!std::isfinite(resi)) { status = 3; break; }
+	}
+	if (status == 0 && step == maxiter) status = 4;
+	stats_out[0] = step; stats_out[1] = status; stats_out[2] = res0; stats_out[3] = resi;
+	return status;
+}
+
+/* TVDRKSolver::solve, aodesolver.cpp:671-765 with initialize_TVDRK_Coeffs
+ * (:45-67), as the reference has it: every stage evaluates the residual of
+ * the step's starting state u (not of the stage state), the time step is
+ * dtmin = min_i dt_i of the first stage, and a stage sets
+ *   ustage = c0 u + c1 ustage - c2 dtmin cfl / A r,   r = -R(u),
+ * until the elapsed time exceeds final_time - 1e-12 (A_SMALL_NUMBER).
+ * out: steps, status (0, or 3 when dtmin is not finite), time */
+int orc_tvdrk(const void *h, int order, double cfl, double final_time, double *u, double *out3)
+{
+	const Disc *d = (const Disc *)h;
+	const Mesh &M = *d->m;
+	const int ne = M.nelem;
+	double co[3][3] = {{1, 0, 1}, {0, 0, 0}, {0, 0, 0}};
+	if (order == 2) { co[1][0] = 0.5; co[1][1] = 0.5; co[1][2] = 0.5; }
+	else if (order == 3) {
+		co[1][0] = 0.75; co[1][1] = 0.25; co[1][2] = 0.25;
+		co[2][0] = 0.3333333333333333; co[2][1] = 0.6666666666666667; co[2][2] = 0.6666666666666667;
+	} else if (order != 1) return 1;
+	std::vector<double> r(4 * (size_t)ne), dtm(ne), us(u, u + 4 * (size_t)ne);
+	Disc::Work w;
+	double time = 0;
+	int step = 0, status = 0;
+	while (time <= final_time - 1e-12) {
+		double dtmin = 0;
+		for (int s = 0; s < order; s++) {
+			std::fill(r.begin(), r.end(), 0.0);
+			d->residual(u, r.data(), true, dtm.data(), w);
+			if (s == 0) dtmin = *std::min_element(dtm.begin(), dtm.end());
+			if (!std::isfinite(dtmin)) { status = 3; break; }
+			for (int i = 0; i < ne; i++)
+				for (int q = 0; q < 4; q++)
+					us[4 * i + q] = co[s][0] * u[4 * i + q] + co[s][1] * us[4 * i + q] -
+					                co[s][2] * dtmin * cfl / M.area[i] * r[4 * i + q];
+		}
+		if (status) break;
+		for (size_t k = 0; k < us.size(); k++) u[k] = us[k];
+		step++;
+		time += dtmin * cfl;
+	}
+	out3[0] = step; out3[1] = status; out3[2] = time;
+	return status;
+}
+
 /* FlowFV_base::computeSurfaceData, flow_spatial.cpp:130-310: returns Cl, CDp, CDsf */
 int orc_surface_data(const void *h, const double *u, int marker, double *out3)
 {
