@@ -44,6 +44,9 @@ STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_tim
 MAIN = dict(cfl_min=50, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
             min_relax=0.2, pc="ilu0", matrix_free=1)
 WORKLOAD = "naca0012_transonic_512x256_ogrid_g1.02_hllc_gg_venkat5"
+# DRAM bytes (read + write) per launch from one ncu capture of this workload
+# (profiles/naca0012_c2_main_solve_launch_list.md; the gradient pass counts k_grad only)
+NCU_DRAM_BYTES = {"face_flux": 44611840, "gradients": 37975808}
 METRIC = "solves/s to ||R||<1e-10 (transonic NACA0012, matrix-free FGMRES, FP32 Jacobian + FP32 block-colour ILU0)"
 
 
@@ -190,6 +193,9 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e_value = world * args.steps / e2e_s
     cl = main.surface_data(ud, 2)[0]
+    u_conv = ud.clone()
+    variants = {} if args.no_variants else run_variants(fv, torch, dev, m, main, start, u0d, prec)
+    ud.copy_(u_conv)
 
     # per-kernel timing (roofline) at the converged state; time shares of one
     # solve from the launch counts per step / per Krylov iteration
@@ -202,7 +208,7 @@ def run_ours(args):
 
     kern = {}
     for name, which in (("residual", 0), ("face_flux", 1), ("jacobian", 2), ("ilu0_apply", 3), ("spmv", 4),
-                        ("ilu0_setup", 5)):
+                        ("ilu0_setup", 5), ("gradients", 6)):
         ms_k, by = timed(S2, which)
         kern[name] = dict(ms=ms_k, bytes=by, gbs=by / (ms_k * 1e-3) / 1e9)
     s1, s2 = stats[-1]
@@ -211,7 +217,12 @@ def run_ours(args):
     calls = {"residual": steps_main + (lin_main if mf else 0), "jacobian": steps_main, "ilu0_setup": steps_main,
              "ilu0_apply": lin_main, "spmv": 0 if mf else lin_main}
     share_ms = {k: calls[k] * kern[k]["ms"] for k in calls}
-    dom = max(share_ms, key=share_ms.get)
+    # the roofline names one kernel: the larger of the residual's two heavy
+    # launches (the face kernel, the gradient/limiter pass) or the ILU(0) sweep
+    single = {"face_flux": calls["residual"] * kern["face_flux"]["ms"],
+              "gradients": calls["residual"] * kern["gradients"]["ms"],
+              "ilu0_apply": share_ms["ilu0_apply"]}
+    dom = max(single, key=single.get)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -244,10 +255,13 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(u0.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": hbm_peak,
-                     "unit": "GB/s", "frac": kern[dom]["gbs"] / hbm_peak, "traffic": None,
-                     "peak_source": peak_src},
+                     "unit": "GB/s", "frac": kern[dom]["gbs"] / hbm_peak,
+                     "traffic": NCU_DRAM_BYTES.get(dom), "peak_source": peak_src,
+                     "note": "FP64-pipe bound (ncu: FP64 pipe 87 % busy, DRAM 4 %)" if dom != "ilu0_apply" else
+                             "latency bound level walk"},
         "kernels": kern,
         "solve_time_shares_ms": share_ms,
+        "variants": variants,
         "residual_gfaces_s": nf / (kern["residual"]["ms"] * 1e-3) / 1e9,
         "jacobian_blocks_s": nblocks / (kern["jacobian"]["ms"] * 1e-3),
         "ilu0_sweep_gbs": kern["ilu0_apply"]["gbs"],
@@ -260,6 +274,45 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def _timed_solve(torch, S_list, u):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    sts = [S.solve(u, raise_on_error=False)[1][0] for S in S_list]
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3, sts[-1]
+
+
+def run_variants(fv, torch, dev, m, main, start, u0d, prec):
+    """The same solve (1) on the plain path: FP64 Jacobian and FP64 ILU(0),
+    freestream start; (2) on the FP32 path warm-started from the converged
+    state of a neighbouring condition (M 0.79), without the starter.  One
+    timed solve each (CUDA events)."""
+    out = {}
+    u = torch.empty_like(u0d)
+    P1 = fv.SteadyBackwardEulerSolver(start, precision=8, **STARTER)
+    P2 = fv.SteadyBackwardEulerSolver(main, precision=8, **MAIN)
+    u.copy_(u0d)
+    t, st = _timed_solve(torch, [P1, P2], u)
+    out["plain_fp64_cold"] = {"solves_s": 1.0 / t, "s_per_solve": t, "main_steps": st["steps"],
+                              "linear_iters": st["lin_iters"], "converged": st["status"] == 0, "res": st["res"]}
+    del P1, P2
+    ph_nb = fv.physics_cfg(**dict(PHYS, Minf=PHYS["Minf"] - 0.01))
+    main_nb = fv.FlowFV(m, ph_nb, fv.numerics_cfg(**NUM_MAIN), BCS)
+    start_nb = fv.FlowFV(m, ph_nb, fv.numerics_cfg(**NUM_START), BCS)
+    u_nb = torch.tensor(np.tile(main_nb.freestream()[0], (m.nelem, 1)), device=dev)
+    fv.SteadyBackwardEulerSolver(start_nb, precision=prec, **STARTER).solve(u_nb, raise_on_error=False)
+    fv.SteadyBackwardEulerSolver(main_nb, precision=prec, **MAIN).solve(u_nb, raise_on_error=False)
+    W = fv.SteadyBackwardEulerSolver(main, precision=prec, **MAIN)
+    u.copy_(u_nb)
+    t, st = _timed_solve(torch, [W], u)
+    out["fp32_warm_from_M0.79"] = {"solves_s": 1.0 / t, "s_per_solve": t, "main_steps": st["steps"],
+                                   "linear_iters": st["lin_iters"], "converged": st["status"] == 0,
+                                   "res": st["res"]}
+    return out
 
 
 def _oracle_case(m):
@@ -355,6 +408,8 @@ def main():
     ap.add_argument("--plain", action="store_true", help="FP64 Jacobian and preconditioner (the plain path)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nvtx", action="store_true", help="profiling aid: NVTX range around each main solve")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the plain-FP64 and warm-start comparison solves")
     ap.add_argument("--no-graph", action="store_true",
                     help="profiling aid: issue every launch from the host instead of replaying a CUDA graph")
     ap.add_argument("--max-main-steps", type=int, default=0,

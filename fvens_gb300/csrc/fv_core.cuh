@@ -115,6 +115,9 @@ struct fv_disc_impl {
 cudaError_t residual_launch(fv_disc_impl *D, const double *u, double *r, int gettimesteps, double *dt,
                             cudaStream_t s);
 cudaError_t gradients_launch(fv_disc_impl *D, const double *u, double *grad, int conserved, cudaStream_t s);
+/* the residual's passes before the face kernel (primitive/ghost states,
+ * gradients, limiter values, WENO blend) into the handle's scratch */
+cudaError_t gradient_pass_launch(fv_disc_impl *D, const double *u, cudaStream_t s);
 /* the face-flux launch alone (reads the prep/gradient/limiter results of the
  * last residual evaluation of the same state) */
 cudaError_t face_launch(fv_disc_impl *D, const double *u, int gettimesteps, cudaStream_t s);

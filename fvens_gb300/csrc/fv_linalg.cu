@@ -790,13 +790,12 @@ __global__ void k_loop_ctrl(Krylov K, int maxit, cudaGraphConditionalHandle h, i
 /* h_i (i <= j) from partials into H[:, j] */
 __global__ void k_reduce_h(Krylov K, int nblk)
 {
-	const int b = blockIdx.x;
+	const int b = blockIdx.x, i = blockIdx.y;  // one warp per (member, basis vector)
 	if (!K.active[b]) return;
 	const int j = *K.jcur;
-	for (int i = 0; i <= j; i++) {
-		const double h = block_sum(K.part + ((size_t)b * (K.restart + 2) + i) * nblk, nblk);
-		if (threadIdx.x == 0) K.H[(size_t)b * (K.restart + 1) * K.restart + (size_t)i * K.restart + j] = h;
-	}
+	if (i > j) return;
+	const double h = block_sum(K.part + ((size_t)b * (K.restart + 2) + i) * nblk, nblk);
+	if (threadIdx.x == 0) K.H[(size_t)b * (K.restart + 1) * K.restart + (size_t)i * K.restart + j] = h;
 }
 
 /* w -= sum_{i<=j} h_i v_i; partial ||w||^2 into part slot restart+1; Z_j = zcur */
@@ -1139,7 +1138,7 @@ static cudaError_t arnoldi_step(Krylov &K, LinOp &op, const Precond &P, int maxi
 	if ((e = precond_apply(P, K.vcur, K.zcur, K.active, s, nk)) != cudaSuccess) return e;
 	if ((e = op.apply(K.zcur, K.w, K.active, s, nk)) != cudaSuccess) return e;
 	k_dot_partial<<<dim3(nb, B, maxit), RBS, 0, s>>>(n, nb, K.V, n, vstep, K.w, n, K.part, 0, m + 2, K.active, K.jcur);
-	k_reduce_h<<<B, 32, 0, s>>>(K, nb);
+	k_reduce_h<<<dim3(B, maxit), 32, 0, s>>>(K, nb);
 	k_cgs_update<<<dim3(nb, B), RBS, 0, s>>>(K, nb);
 	k_givens<<<B, 32, 0, s>>>(K, nb, maxit);
 	k_next_basis<<<dim3((unsigned)((n + 255) / 256), B), 256, 0, s>>>(K);

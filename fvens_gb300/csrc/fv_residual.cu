@@ -93,38 +93,48 @@ cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cud
 	return cudaGetLastError();
 }
 
-cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int gettimesteps, double *dt, cudaStream_t s)
+/* the residual's passes before the face kernel: primitive and ghost states,
+ * gradients (+ Barth-Jespersen / Venkatakrishnan limiter values), WENO blend */
+cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
 	const int B = Dh->batch;
 	auto grid = [&](int n) { return dim3((unsigned)((n + BS - 1) / BS), (unsigned)B); };
 	int nk = 0;
-	if (D.order2) {
-		k_prep<<<grid(D.nelem + D.nbface), BS, 0, s>>>(D, u, Dh->w);
+	k_prep<<<grid(D.nelem + D.nbface), BS, 0, s>>>(D, u, Dh->w);
+	nk++;
+	if (D.gradscheme != GRAD_NONE) {
+		const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
+		k_grad<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, lim);
 		nk++;
-		if (D.gradscheme != GRAD_NONE) {
-			const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
-			k_grad<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, lim);
+		if (D.recon == REC_WENO) {
+			k_weno<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.grad, Dh->w.lgrad);
 			nk++;
-			if (D.recon == REC_WENO) {
-				k_weno<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.grad, Dh->w.lgrad);
-				nk++;
-			}
-		} else {
-			cudaMemsetAsync(Dh->w.grad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
-			if (D.recon == REC_WENO) cudaMemsetAsync(Dh->w.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
-			if (D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN) {
-				// zero gradients: every face value equals the cell value, the limiter is 1
-				k_grad<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, 0);
-				nk++;
-			}
+		}
+	} else {
+		cudaMemsetAsync(Dh->w.grad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
+		if (D.recon == REC_WENO) cudaMemsetAsync(Dh->w.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
+		if (D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN) {
+			// zero gradients: every face value equals the cell value, the limiter is 1
+			k_grad<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, 0);
+			nk++;
 		}
 	}
-	face_launch(Dh, u, gettimesteps, s);
-	nk++;
-	k_gather<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
-	nk++;
 	Dh->kernels_launched += nk;
+	return cudaGetLastError();
+}
+
+cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int gettimesteps, double *dt, cudaStream_t s)
+{
+	const DiscDev &D = Dh->d;
+	auto grid = [&](int n) { return dim3((unsigned)((n + BS - 1) / BS), (unsigned)Dh->batch); };
+	if (D.order2) {
+		const cudaError_t e = gradient_pass_launch(Dh, u, s);
+		if (e) return e;
+	}
+	face_launch(Dh, u, gettimesteps, s);
+	k_gather<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
+	Dh->kernels_launched += 2;
 	return cudaGetLastError();
 }
 

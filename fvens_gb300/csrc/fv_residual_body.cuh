@@ -124,25 +124,28 @@ FV_HD void grad_body(const DiscDev &D, int b, int i, const d4 *__restrict__ q, c
 			if (d > dmax) dmax = d;
 			if (d < dmin) dmin = d;
 		}
-		double l = 1.0;
+		// the smallest of 1 and the faces' ratios num/den (den > 0), found by
+		// comparing cross products so that only the winner is divided
+		double bn = 1.0, bd = 1.0;
 		for (int j = 0; j < 4; j++) {
 			if (fl[j] < 0) continue;
 			double uf = uv;
 			uf += 1.0 * gr[2 * v] * dx[j];
 			uf += 1.0 * gr[2 * v + 1] * dy[j];
 			const double dm = uf - uv;
-			double ph;
+			double num, den;
 			if (venkat) {
 				const double dp = dm < 0 ? dmin : dmax;
-				ph = (dp * dp + 2 * dp * dm + eps2) / (dp * dp + dp * dm + 2 * dm * dm + eps2);
+				num = dp * dp + 2 * dp * dm + eps2;
+				den = dp * dp + dp * dm + 2 * dm * dm + eps2;
 			} else {
-				if (dm > 0) ph = fmin(1.0, dmax / dm);
-				else if (dm < 0) ph = fmin(1.0, dmin / dm);
-				else ph = 1.0;
+				if (dm == 0) continue;  // ratio 1
+				num = dm > 0 ? dmax : -dmin;
+				den = dm > 0 ? dm : -dm;
 			}
-			if (ph < l) l = ph;
+			if (num * bd < bn * den) { bn = num; bd = den; }
 		}
-		setc(lim, v, l);
+		setc(lim, v, bn == bd ? 1.0 : bn / bd);
 	}
 	phi[(size_t)b * D.nelem + i] = lim;
 }

@@ -248,7 +248,8 @@ fv_status fv_solver_history(const fv_solver *s, int member, int maxn, double *re
 /* kernels launched by one pseudo-time step (all members) */
 long long fv_solver_kernels_per_step(const fv_solver *s);
 /* Times one hot-path launch sequence in isolation with CUDA events on the
- * handle's stream (3 warm-up launches, then reps timed ones) at state d_u;
+ * handle's stream (3 warm-up launches, then reps timed ones, each after a
+ * 256 MB write that evicts L2) at state d_u;
  * *avg_ms = mean duration, *bytes = compulsory (algorithmic) bytes of one
  * launch for the roofline.  Synchronises. */
 #define FV_KERNEL_RESIDUAL 0        /* whole residual evaluation */
@@ -257,6 +258,7 @@ long long fv_solver_kernels_per_step(const fv_solver *s);
 #define FV_KERNEL_PRECOND_APPLY 3   /* one preconditioner application */
 #define FV_KERNEL_SPMV 4            /* block SpMV */
 #define FV_KERNEL_PRECOND_SETUP 5   /* factorisation */
+#define FV_KERNEL_GRADIENTS 6       /* residual passes before the face kernel (states, gradients, limiter) */
 fv_status fv_solver_time_kernel(fv_solver *s, const double *d_u, int which, int reps, double *avg_ms, double *bytes);
 
 /* ---- explicit time stepping ---- */
