@@ -1,0 +1,46 @@
+"""Writes the reference's regression meshes as compact arrays for the tests
+(the reference tree is not available where the GPU tests run).
+
+    python tests/golden/make_reference_meshes.py [REFERENCE_ROOT]
+
+Reads, with this project's own Gmsh 2.2 reader (cells kept in file order):
+  testcases/naca0012/grids/naca0012luo.msh                 -> naca0012luo_mesh.npz
+  testcases/visc-naca0012/grids/NACA0012_lam_hybrid_1.msh  -> naca0012_lam_hybrid_1_mesh.npz
+The functional-regression values the tests compare with are the reference's
+files testcases/naca0012/regr-MUSCL_LeastSquares_HLLC.txt and
+testcases/visc-naca0012/regr-LeastSquares_Roe.txt, stored alongside.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import fvens_gb300 as fv  # noqa: E402
+
+CASES = [
+    ("testcases/naca0012/grids/naca0012luo.msh", "naca0012luo_mesh.npz",
+     "testcases/naca0012/regr-MUSCL_LeastSquares_HLLC.txt"),
+    ("testcases/visc-naca0012/grids/NACA0012_lam_hybrid_1.msh", "naca0012_lam_hybrid_1_mesh.npz",
+     "testcases/visc-naca0012/regr-LeastSquares_Roe.txt"),
+]
+
+
+def main(root):
+    for msh, out, regr in CASES:
+        m = fv.UMesh.read_gmsh(os.path.join(root, msh), reorder=0)
+        e = m.export()
+        with open(os.path.join(root, regr)) as f:
+            vals = f.read().split()
+        cl, cdp = float(vals[0]), float(vals[1])
+        cdsf = float(vals[2]) if vals[2].lower().lstrip("-") != "nan" else np.nan
+        np.savez_compressed(os.path.join(HERE, out), coords=e["coords"], nnode=e["nnode"].astype(np.int8),
+                            inpoel=e["inpoel"], bface=e["bface"], btag=e["btag"].astype(np.int16),
+                            regression=np.array([cl, cdp, cdsf]))
+        print(out, m.nelem, "cells", m.npoin, "points", m.nbface, "boundary faces", "regression", cl, cdp, cdsf)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,45 @@
+"""The reference's functional-regression cases on the reference's own meshes
+(arrays in tests/golden/, written by tests/golden/make_reference_meshes.py),
+with the control-file settings of the reference's test runs:
+  testcases/naca0012/transonic-sanity-test-muscl.ctrl + opts.solverc
+  testcases/visc-naca0012/laminar-implicit.ctrl + opts.solverc"""
+import os
+
+import numpy as np
+
+import fvens_gb300 as fv
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+CASES = {
+    # HLLC, least squares, MUSCL Van Albada; starter CFL 50-1000, 20 steps, tol 1e-1;
+    # main CFL 500-5000, tol 1e-7, 170 steps; robust_flow update; -pc_type sor
+    "inviscid_naca0012luo": dict(
+        mesh="naca0012luo_mesh.npz", bcs=[(2, "slipwall", ()), (4, "farfield", ())],
+        phys=dict(Minf=0.8, aoa_deg=1.25),
+        start=dict(flux="HLLC", gradient="NONE"),
+        main=dict(flux="HLLC", gradient="LEASTSQUARES", reconstruction="VANALBADA", limiter_param=20.0),
+        start_solver=dict(cfl_min=50, cfl_max=1000, tolerance=1e-1, max_timesteps=20),
+        main_solver=dict(cfl_min=500, cfl_max=5000, tolerance=1e-7, max_timesteps=170),
+        pc="sgs", nl_update="robust_flow"),
+    # Roe, least squares, no limiter, laminar (Re 5000, Sutherland); starter CFL
+    # 200-1000, 50 steps, tol 1e-1; main CFL 500-5000, tol 1e-6, 80 steps; full
+    # update; -pc_type bjacobi -sub_pc_type ilu
+    "laminar_naca0012_hybrid1": dict(
+        mesh="naca0012_lam_hybrid_1_mesh.npz", bcs=[(4, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))],
+        phys=dict(Minf=0.5, aoa_deg=0.0, Reinf=5000.0, Tinf=288.15, Pr=0.72, viscous=True),
+        start=dict(flux="ROE", gradient="NONE"),
+        main=dict(flux="ROE", gradient="LEASTSQUARES"),
+        start_solver=dict(cfl_min=200, cfl_max=1000, tolerance=1e-1, max_timesteps=50),
+        main_solver=dict(cfl_min=500, cfl_max=5000, tolerance=1e-6, max_timesteps=80),
+        pc="ilu0", nl_update="full"),
+}
+
+
+def load(name):
+    """(UMesh with RCM ordering as -mesh_reorder rcm, case dict, regression (CL, CDp, CDsf))."""
+    c = CASES[name]
+    z = np.load(os.path.join(GOLDEN, c["mesh"]))
+    m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
+                             z["btag"].astype(np.int32), reorder=1)
+    return m, c, z["regression"]

@@ -1,0 +1,45 @@
+"""The oracle against the reference's functional-regression values on the
+reference's own meshes and control settings (testcases/naca0012 and
+testcases/visc-naca0012; values in their regr-*.txt files).  The reference
+stops at a relative residual drop of 1e-7 / 1e-6 and compares CL to 1e-6 and
+CDp, CDsf to 1e-8 against runs of its own code path; the oracle follows the
+same algorithm with its own (natural-order) ILU(0)/SGS, so its drag
+coefficients at the same stopping tolerance agree to a few 1e-7."""
+import numpy as np
+import pytest
+
+from oracle import orc
+from tests import regression_cases as rc
+
+
+def _oracle_solve(name, tol=None, abs_tol=False, maxiter=None):
+    m, c, regr = rc.load(name)
+    om = orc.Mesh.from_export(m.export())
+    d1 = orc.Disc(om, **c["phys"], **c["start"], bcs=c["bcs"])
+    d2 = orc.Disc(om, **c["phys"], **c["main"], bcs=c["bcs"])
+    u0 = np.tile(d2.freestream(), (m.nelem, 1))
+    s1, s2 = c["start_solver"], c["main_solver"]
+    u1, _ = d1.steady_solve(u0, cflmin=s1["cfl_min"], cflmax=s1["cfl_max"], tol=s1["tolerance"],
+                            maxiter=s1["max_timesteps"], abs_tol=False, pc=c["pc"], nl_update=c["nl_update"])
+    u2, st = d2.steady_solve(u1, cflmin=s2["cfl_min"], cflmax=s2["cfl_max"], tol=tol or s2["tolerance"],
+                             maxiter=maxiter or s2["max_timesteps"], abs_tol=abs_tol, pc=c["pc"],
+                             nl_update=c["nl_update"])
+    return st, d2.surface_data(u2, 2), regr
+
+
+def test_oracle_reproduces_inviscid_naca0012_regression():
+    st, f, regr = _oracle_solve("inviscid_naca0012luo")
+    assert st["status"] == 0 and st["steps"] <= 170
+    assert abs(f[0] - regr[0]) <= 1e-6 * abs(regr[0])      # the reference's CL tolerance
+    assert abs(f[1] - regr[1]) <= 3e-7 * abs(regr[1])      # CDp
+    assert f[2] == 0.0                                      # inviscid: no skin friction
+
+
+def test_oracle_reproduces_laminar_naca0012_regression():
+    st, f, regr = _oracle_solve("laminar_naca0012_hybrid1")
+    assert st["status"] == 0 and st["steps"] <= 80
+    assert abs(f[1] - regr[1]) <= 5e-7 * abs(regr[1])      # CDp
+    assert abs(f[2] - regr[2]) <= 5e-7 * abs(regr[2])      # CDsf
+    # CL of the symmetric aerofoil at zero incidence is mesh-asymmetry noise
+    # (3e-5): compared in absolute terms
+    assert abs(f[0] - regr[0]) <= 1e-7
