@@ -41,7 +41,7 @@ NUM_START = dict(flux="HLLC", gradient="NONE")
 BCS = [(2, "slipwall", ()), (4, "farfield", ())]
 STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
                min_relax=0.2, pc="ilu0")
-MAIN = dict(cfl_min=50, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
+MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
             min_relax=0.2, pc="ilu0", matrix_free=1)
 WORKLOAD = "naca0012_transonic_512x256_ogrid_g1.02_hllc_gg_venkat5"
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
