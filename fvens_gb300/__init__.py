@@ -142,6 +142,13 @@ class UMesh:
         check(lib().fv_mesh_read_gmsh(path.encode(), int(reorder), ctypes.byref(h)))
         return cls(h)
 
+    @classmethod
+    def read(cls, path, reorder=0):
+        """Gmsh 2.2 (.msh) or SU2 (.su2) by extension (the reference's readMesh)."""
+        h = ctypes.c_void_p()
+        check(lib().fv_mesh_read(path.encode(), int(reorder), ctypes.byref(h)))
+        return cls(h)
+
     def export(self):
         coords = np.zeros((self.npoin, 2))
         nnode = np.zeros(self.nelem, np.int32)
@@ -246,6 +253,12 @@ class FlowFV:
         if raise_on_error:
             check(rc)
         return rc, steps, tm
+
+    def entropy_error(self, u):
+        """FlowOutput::compute_entropy_cell per batch member."""
+        out = np.zeros(self.batch)
+        check(lib().fv_entropy_error(self._h, _vp(dptr(u)), _hp(out, ctypes.c_double)))
+        return out
 
     def surface_data(self, u, wall_marker):
         """(Cl, CDp, CDsf) over the faces of wall_marker, one row per batch member
@@ -403,6 +416,31 @@ class SteadyBackwardEulerSolver:
                                       _hp(lin, ctypes.c_int), ctypes.byref(n)))
         k = n.value
         return res[:k], cfl[:k], lin[:k]
+
+    def write_convergence_history(self, path_or_file, member=0, wall_time=None):
+        """Writes the convergence history of one member in the reference's
+        format (writeConvergenceHistoryHeader / writeStepToConvergenceHistory,
+        aoutput.cpp:617-636): step, log10 relative and absolute residual,
+        total and linear wall time, linear iterations (cumulative), CFL.  The
+        device loop keeps no per-step clock: the time columns hold the solve's
+        wall time spread evenly over its steps when wall_time is given, else 0."""
+        res, cfl, lin = self.history(member)
+        n = len(res)
+        lines = ["#%6s%14s%14s%12s%12s%12s%10s" % ("NStep", "Log rel resi", "Log abs resi", "Tot.Wtime",
+                                                   "Lin.Wtime", "Lin.iters", "CFL"),
+                 "#" + "-" * 82]
+        total = 0
+        for k in range(n):
+            total += int(lin[k])
+            t = (wall_time * (k + 1) / n) if wall_time else 0.0
+            lines.append("%7d%14.6g%14.6g%12.4g%12.4g%12d%10.4g" % (
+                k + 1, np.log10(res[k] / res[0]), np.log10(res[k]), t, 0.0, total, cfl[k]))
+        text = "\n".join(lines) + "\n"
+        if hasattr(path_or_file, "write"):
+            path_or_file.write(text)
+        else:
+            with open(path_or_file, "w") as f:
+                f.write(text)
 
     def kernels_per_step(self):
         L = lib()

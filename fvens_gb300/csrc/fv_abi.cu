@@ -188,6 +188,31 @@ fv_status fv_mesh_read_gmsh(const char *path, int reorder, fv_mesh **out)
 	return finish_mesh(m, rc, err, out);
 }
 
+fv_status fv_mesh_read_su2(const char *path, int reorder, fv_mesh **out)
+{
+	if (!path || !out) { set_error("null argument"); return FV_ERR_INVALID; }
+	RawMesh r;
+	std::string err;
+	if (read_su2(path, r, &err)) { set_error(err); return FV_ERR_MESH; }
+	fv_mesh *m = new fv_mesh();
+	const int rc = mesh_from_arrays(m->h, r.npoin, r.coords.data(), r.nelem, r.nnode.data(), r.inpoel.data(), r.nbface,
+	                                r.bface.data(), r.btag.data(), reorder, &err);
+	return finish_mesh(m, rc, err, out);
+}
+
+/* readMesh (meshreaders.cpp:33-50): the format from the file extension */
+fv_status fv_mesh_read(const char *path, int reorder, fv_mesh **out)
+{
+	if (!path || !out) { set_error("null argument"); return FV_ERR_INVALID; }
+	const std::string p(path);
+	const size_t dot = p.rfind('.');
+	const std::string ext = dot == std::string::npos ? "" : p.substr(dot + 1);
+	if (ext == "msh") return fv_mesh_read_gmsh(path, reorder, out);
+	if (ext == "su2") return fv_mesh_read_su2(path, reorder, out);
+	set_error("unknown mesh file extension: " + ext);
+	return FV_ERR_INVALID;
+}
+
 fv_status fv_mesh_counts(const fv_mesh *m, int c[6])
 {
 	if (!m || !c) { set_error("null argument"); return FV_ERR_INVALID; }

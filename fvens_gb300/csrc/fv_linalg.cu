@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(BS) k_diag_setup(int nelem, const RA *__restri
 	RA tmp[16];
 	load_blk(Ab + (size_t)i * 16, tmp);
 	for (int q = 0; q < 16; q++) blk[q] = R(tmp[q]);
-	if (!inv4(blk, inv)) { atomicOr(err, 1); for (int q = 0; q < 16; q++) inv[q] = R(0); }
+	if (!inv4(blk, inv)) { atomicOr(err + b, 1); for (int q = 0; q < 16; q++) inv[q] = R(0); }
 	store_blk(Dinv + ((size_t)b * N + p) * 16, inv);
 	if (copy_rows) {
 		R *Fb = F + (size_t)b * 5 * N * 16;
@@ -173,7 +173,7 @@ __device__ __forceinline__ void ilu_row(int nelem, int p, int b, const RA *__res
 		}
 	}
 	R inv[16];
-	if (!inv4(row[0], inv)) { atomicOr(err, 1); for (int q = 0; q < 16; q++) inv[q] = R(0); }
+	if (!inv4(row[0], inv)) { atomicOr(err + b, 1); for (int q = 0; q < 16; q++) inv[q] = R(0); }
 	store_blk(Db + (size_t)p * 16, inv);
 	for (int s = 0; s < 5; s++) store_blk(Fb + ((size_t)s * N + p) * 16, row[s]);
 }
@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(PT) k_ilu_parts(int nelem, int part0, int cap,
 					R dblk[16], inv[16];
 					for (int q = 0; q < 16; q++) dblk[q] = sRow[(size_t)c * 80 + q];
 					if (!inv4(dblk, inv)) {
-						if (row == 0) atomicOr(err, 1);
+						if (row == 0) atomicOr(err + b, 1);
 						for (int q = 0; q < 16; q++) inv[q] = R(0);
 					}
 					for (int m = 0; m < 4; m++) sD[(size_t)c * 16 + 4 * row + m] = inv[4 * row + m];

@@ -47,8 +47,8 @@ constexpr int kMaxPartSize = 256;
 cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec, int ordering = 1,
                           int part_size = 128);
 void precond_free(Precond &P);
-/* factorisation / diagonal inversion from P.A; err_flag (device int) is set
- * non-zero when a diagonal block is singular */
+/* factorisation / diagonal inversion from P.A; err_flag[b] (device ints, one
+ * per batch member) is set non-zero when a diagonal block of member b is singular */
 cudaError_t precond_setup(Precond &P, int *err_flag, const int *active, cudaStream_t s, int *nk);
 /* z = M^{-1} r, FP64 vectors in cell order [batch][nelem][4] */
 cudaError_t precond_apply(const Precond &P, const double *r, double *z, const int *active, cudaStream_t s, int *nk);

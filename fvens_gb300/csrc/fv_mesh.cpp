@@ -505,6 +505,103 @@ RawMesh gen_naca_ogrid(int nc, int nr, double rfar, int nbl, double h0, double g
 	return r;
 }
 
+namespace {
+/* next "KEY=value" header of an SU2 file: the value as an integer (tags and
+ * counts are numeric in the meshes this reader supports) */
+bool su2_header(std::istream &in, const char *key, long &value, std::string *err)
+{
+	std::string tok;
+	while (in >> tok) {
+		const size_t eq = tok.find('=');
+		if (eq == std::string::npos) continue;
+		if (tok.compare(0, eq, key) != 0) continue;
+		std::string v = tok.substr(eq + 1);
+		if (v.empty() && !(in >> v)) break;
+		try {
+			value = std::stol(v);
+		} catch (...) {
+			if (err) *err = std::string("SU2: non-numeric value of ") + key + ": " + v;
+			return false;
+		}
+		return true;
+	}
+	if (err) *err = std::string("SU2: missing ") + key;
+	return false;
+}
+}  // namespace
+
+int read_su2(const std::string &path, RawMesh &out, std::string *err)
+{
+	std::ifstream in(path);
+	if (!in) {
+		if (err) *err = "cannot open " + path;
+		return 1;
+	}
+	out = RawMesh();
+	long ndim = 0, nelem = 0, npoin = 0, nmark = 0;
+	if (!su2_header(in, "NDIME", ndim, err)) return 2;
+	if (ndim != 2) {
+		if (err) *err = "SU2: mesh is not 2-dimensional";
+		return 2;
+	}
+	if (!su2_header(in, "NELEM", nelem, err)) return 2;
+	out.nelem = (int)nelem;
+	out.nnode.resize(nelem);
+	out.inpoel.assign(4 * (size_t)nelem, -1);
+	for (long k = 0; k < nelem; k++) {
+		int type;
+		if (!(in >> type)) { if (err) *err = "SU2: truncated element list"; return 3; }
+		const int nn = type == 5 ? 3 : type == 9 ? 4 : 0;
+		if (!nn) {
+			if (err) *err = "SU2: unknown element type " + std::to_string(type);
+			return 3;
+		}
+		out.nnode[k] = nn;
+		for (int q = 0; q < nn; q++) in >> out.inpoel[4 * k + q];
+		long idx;
+		in >> idx;
+	}
+	if (!su2_header(in, "NPOIN", npoin, err)) return 2;
+	out.npoin = (int)npoin;
+	out.coords.resize(2 * (size_t)npoin);
+	{
+		// each point line: x y [index]; the index is optional
+		std::string line;
+		std::getline(in, line);
+		for (long k = 0; k < npoin; k++) {
+			if (!std::getline(in, line)) { if (err) *err = "SU2: truncated point list"; return 3; }
+			std::istringstream ls(line);
+			if (!(ls >> out.coords[2 * k] >> out.coords[2 * k + 1])) {
+				if (err) *err = "SU2: bad point line " + std::to_string(k);
+				return 3;
+			}
+		}
+	}
+	if (!su2_header(in, "NMARK", nmark, err)) return 2;
+	for (long mk = 0; mk < nmark; mk++) {
+		long tag = 0, ne = 0;
+		if (!su2_header(in, "MARKER_TAG", tag, err)) return 2;
+		if (!su2_header(in, "MARKER_ELEMS", ne, err)) return 2;
+		for (long k = 0; k < ne; k++) {
+			int type, a, b;
+			if (!(in >> type >> a >> b) || type != 3) {
+				if (err) *err = "SU2: boundary elements must be lines (type 3)";
+				return 3;
+			}
+			out.bface.push_back(a);
+			out.bface.push_back(b);
+			out.btag.push_back((int)tag);
+		}
+	}
+	out.nbface = (int)out.btag.size();
+	for (int v : out.inpoel)
+		if (v >= (int)npoin) {
+			if (err) *err = "SU2: node index out of range";
+			return 4;
+		}
+	return 0;
+}
+
 int read_gmsh2(const std::string &path, RawMesh &out, std::string *err)
 {
 	std::ifstream in(path);

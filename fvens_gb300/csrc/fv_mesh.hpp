@@ -100,4 +100,9 @@ RawMesh gen_naca_ogrid(int nc, int nr, double rfar, int nbl, double h0, double g
  * their first tag as marker; triangles (2) and quads (3) are cells. */
 int read_gmsh2(const std::string &path, RawMesh &out, std::string *err);
 
+/* SU2 ASCII reader (2-D): NELEM cells (VTK types 5 triangle, 9 quad, 0-based
+ * node indices), NPOIN coordinates, NMARK markers with numeric MARKER_TAG whose
+ * line elements (type 3) are boundary faces. */
+int read_su2(const std::string &path, RawMesh &out, std::string *err);
+
 }  // namespace fvg

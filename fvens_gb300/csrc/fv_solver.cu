@@ -37,7 +37,7 @@ constexpr int RBS = 256;
 struct StepState {
 	double *res, *resold, *res0, *cfl, *pm;  // [batch]
 	int *step, *status, *active;              // [batch]
-	int *pc_err;                              // [1]
+	int *pc_err;                              // [batch] singular preconditioner block
 	double *hist;                             // [maxiter][batch][3]: res, cfl, linear iterations
 	int *linits;                              // [batch] cumulative linear iterations
 };
@@ -156,7 +156,7 @@ __global__ void k_norm(int B, int nblk, const double *__restrict__ part, StepSta
 		double *h = S.hist + ((size_t)step * B + b) * 3;
 		h[0] = res; h[1] = S.cfl[b]; h[2] = kiters[b];
 	}
-	if (*S.pc_err) {
+	if (S.pc_err[b]) {
 		S.status[b] = ST_PRECOND;
 		S.active[b] = 0;
 		S.step[b] = step + 1;
@@ -183,8 +183,8 @@ __global__ void k_norm(int B, int nblk, const double *__restrict__ part, StepSta
 __global__ void k_init(int B, StepState S, const int *__restrict__ mask)
 {
 	const int b = blockIdx.x * blockDim.x + threadIdx.x;
-	if (b == 0) *S.pc_err = 0;
 	if (b >= B) return;
+	S.pc_err[b] = 0;
 	S.res[b] = 1.0; S.resold[b] = 1.0; S.res0[b] = 1.0; S.cfl[b] = 0.0;
 	S.step[b] = 0; S.linits[b] = 0;
 	const int on = mask ? mask[b] : 1;
@@ -378,8 +378,8 @@ fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, int ordering, in
 	p->M = M;
 	cudaError_t e = precond_alloc(p->P, D->mesh, D->batch, type, M->A.prec, ordering ? 1 : 0, part_size > 0 ? part_size : 128);
 	p->P.A = &M->A;
-	if (!e) e = cudaMalloc(&p->err, sizeof(int));
-	if (!e) e = cudaMemset(p->err, 0, sizeof(int));
+	if (!e) e = cudaMalloc(&p->err, sizeof(int) * D->batch);
+	if (!e) e = cudaMemset(p->err, 0, sizeof(int) * D->batch);
 	if (e) {
 		fv_precond_destroy(p);
 		return cuda_status(e, "preconditioner allocation");
@@ -401,15 +401,16 @@ fv_status fv_precond_setup(fv_precond *p)
 {
 	if (!p) { set_error("null argument"); return FV_ERR_INVALID; }
 	int nk = 0;
-	cudaError_t e = cudaMemsetAsync(p->err, 0, sizeof(int), p->D->stream);
+	const int B = p->D->batch;
+	cudaError_t e = cudaMemsetAsync(p->err, 0, sizeof(int) * B, p->D->stream);
 	if (!e) e = precond_setup(p->P, p->err, nullptr, p->D->stream, &nk);
 	count_launches(nk);
 	if (e) return cuda_status(e, "preconditioner setup");
-	int herr = 0;
-	e = cudaMemcpyAsync(&herr, p->err, sizeof(int), cudaMemcpyDeviceToHost, p->D->stream);
+	std::vector<int> herr(B, 0);
+	e = cudaMemcpyAsync(herr.data(), p->err, sizeof(int) * B, cudaMemcpyDeviceToHost, p->D->stream);
 	if (!e) e = cudaStreamSynchronize(p->D->stream);
 	if (e) return cuda_status(e, "preconditioner setup");
-	if (herr) {
+	if (std::any_of(herr.begin(), herr.end(), [](int v) { return v != 0; })) {
 		set_error("singular diagonal block in the preconditioner");
 		return FV_ERR_NUMERICAL;
 	}
@@ -521,7 +522,7 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	if (!e) e = salloc(S, &S->S.step, B);
 	if (!e) e = salloc(S, &S->S.status, B);
 	if (!e) e = salloc(S, &S->S.active, B);
-	if (!e) e = salloc(S, &S->S.pc_err, 1);
+	if (!e) e = salloc(S, &S->S.pc_err, B);
 	if (!e) e = salloc(S, &S->S.linits, B);
 	if (!e) e = salloc(S, &S->S.hist, 3 * (size_t)cfg->max_timesteps * B);
 	if (!e && cfg->matrix_free) {

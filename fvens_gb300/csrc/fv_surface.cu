@@ -15,7 +15,15 @@
  *   CDsf = sum Cf (t . w) len / sum len
  * The sums are a fixed-order tree reduction (one CTA per member), so results
  * are bitwise reproducible.
+ *
+ * Also the entropy error sqrt(sum_i ((s_i - s_inf)/s_inf)^2 A_i), s = p/rho^gamma
+ * (FlowOutput::compute_entropy_cell, aoutput.cpp:28-62), the accuracy measure
+ * of the reference's grid-convergence tests.
  */
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "fv_abi_internal.hpp"
@@ -77,10 +85,57 @@ __global__ void __launch_bounds__(SBS) k_surface(DiscDev D, const double *__rest
 	if (threadIdx.x < 4) out[4 * b + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+/* entropy error partials: sum over cells of ((s - s_inf)/s_inf)^2 A, s = p / rho^gamma
+ * (FlowOutput::compute_entropy_cell, aoutput.cpp:28-62) */
+__global__ void __launch_bounds__(SBS) k_entropy_partial(DiscDev D, const double *__restrict__ u, int nblk,
+                                                         double *__restrict__ part)
+{
+	const int b = blockIdx.y;
+	const Phys P = D.phys[b];
+	const double sinf = P.pinf_cons / pow(P.uinf[0], P.g);  // entropy of the freestream state
+	double acc = 0;
+	for (int i = blockIdx.x * SBS + threadIdx.x; i < D.nelem; i += nblk * SBS) {
+		const d4 uc = reinterpret_cast<const d4 *>(u)[(size_t)b * D.nelem + i];
+		const double p = P.gm1 * (uc.w - 0.5 * (uc.y * uc.y + uc.z * uc.z) / uc.x);
+		const double e = (p / pow(uc.x, P.g) - sinf) / sinf;
+		acc += e * e * D.area[i];
+	}
+	__shared__ double sh[SBS];
+	sh[threadIdx.x] = acc;
+	__syncthreads();
+	for (int o = SBS / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) part[(size_t)b * nblk + blockIdx.x] = sh[0];
+}
+
 }  // namespace
 }  // namespace fvg
 
 using namespace fvg;
+
+extern "C" fv_status fv_entropy_error(fv_disc *D, const double *u, double *h_err)
+{
+	if (!D || !u || !h_err) { set_error("null argument"); return FV_ERR_INVALID; }
+	const int B = D->batch;
+	const int nblk = std::max(1, std::min(256, (D->d.nelem + SBS * 8 - 1) / (SBS * 8)));
+	double *part = reinterpret_cast<double *>(D->w.fflux);  // residual scratch: >= 4 * naface doubles per member
+	if ((size_t)nblk > 4 * (size_t)D->d.naface) { set_error("mesh too small for the entropy reduction"); return FV_ERR_INVALID; }
+	k_entropy_partial<<<dim3(nblk, B), SBS, 0, D->stream>>>(D->d, u, nblk, part);
+	count_launches(1);
+	std::vector<double> h((size_t)nblk * B);
+	cudaError_t e = cudaGetLastError();
+	if (!e) e = cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, D->stream);
+	if (!e) e = cudaStreamSynchronize(D->stream);
+	if (e) return cuda_status(e, "entropy error");
+	for (int b = 0; b < B; b++) {
+		double s = 0;
+		for (int k = 0; k < nblk; k++) s += h[(size_t)b * nblk + k];
+		h_err[b] = sqrt(s);
+	}
+	return FV_OK;
+}
 
 extern "C" fv_status fv_surface_data(fv_disc *D, const double *u, int marker, double *h_out)
 {

@@ -105,6 +105,10 @@ fv_status fv_mesh_create(const fv_mesh_desc *desc, int reorder, fv_mesh **out);
 fv_status fv_mesh_generate(int kind, const double *params, int nparams, int reorder, fv_mesh **out);
 /* Gmsh 2.2 ASCII (meshreaders.cpp:66-265) */
 fv_status fv_mesh_read_gmsh(const char *path, int reorder, fv_mesh **out);
+/* SU2 ASCII, 2-D, numeric marker tags (meshreaders.cpp:267-397) */
+fv_status fv_mesh_read_su2(const char *path, int reorder, fv_mesh **out);
+/* readMesh (meshreaders.cpp:33-50): .msh (Gmsh) or .su2 by extension */
+fv_status fv_mesh_read(const char *path, int reorder, fv_mesh **out);
 /* counts: nelem, nbface, ninface, naface, npoin, ncolors */
 fv_status fv_mesh_counts(const fv_mesh *m, int counts[6]);
 /* The mesh as built (cells in their final order, boundary faces oriented);
@@ -166,6 +170,10 @@ fv_status fv_get_gradients(fv_disc *d, const double *d_u, double *d_grad, int pr
  * wall_marker, from the cell-centred state and its conserved gradients, FP64.
  * h_out[3*batch] = (Cl, CDp, CDsf) per condition (host).  Synchronises. */
 fv_status fv_surface_data(fv_disc *d, const double *d_u, int wall_marker, double *h_out);
+/* FlowOutput::compute_entropy_cell (aoutput.cpp:28-62): sqrt(sum_i
+ * ((s_i - s_inf)/s_inf)^2 A_i), s = p / rho^gamma, per condition into
+ * h_err[batch] (host).  Uses the residual scratch.  Synchronises. */
+fv_status fv_entropy_error(fv_disc *d, const double *d_u, double *h_err);
 
 /* ---- Jacobian: Spatial::assemble_jacobian (aspatial.cpp:242-340) ---- */
 /* precision 4: FP32 blocks, 8: FP64 blocks */

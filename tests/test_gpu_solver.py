@@ -104,3 +104,44 @@ def test_host_buffer_solve(cuda):
     S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200, precision=4)
     rc, st = S.solve_host(u)
     assert st[0]["status"] == 0 and np.all(np.isfinite(u))
+
+
+def test_convergence_history_file_format(cuda, tmp_path):
+    """The reference's convergence-history columns (aoutput.cpp:617-636), as
+    read by its plotting scripts with numpy.genfromtxt."""
+    import torch
+    m, gd, od = _setup()
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200, precision=4)
+    rc, st = S.solve(torch.tensor(u0, device=cuda))
+    path = tmp_path / "conv.log"
+    S.write_convergence_history(str(path), wall_time=1.0)
+    data = np.genfromtxt(str(path))
+    assert data.shape == (st[0]["steps"], 7)
+    assert data[0, 0] == 1 and data[-1, 0] == st[0]["steps"]
+    assert data[0, 1] == 0.0 and abs(data[-1, 2] - np.log10(st[0]["res"])) < 1e-5
+    assert data[-1, 5] == st[0]["lin_iters"] and data[0, 6] == 10.0
+
+
+def test_batch_member_failure_is_isolated(cuda):
+    """A member that diverges (negative energy injected in its initial state,
+    on the host) ends with FV_ERR_NUMERICAL; the other members still converge
+    to the same state as their single solves."""
+    import torch
+    m = cases.channel(48, 16)
+    plist = [dict(Minf=0.5), dict(Minf=0.45), dict(Minf=0.4, aoa_deg=1.0)]
+    gd = fv.FlowFV(m, [fv.physics_cfg(**p) for p in plist], fv.numerics_cfg(flux="ROE"), cases.CHANNEL_BCS)
+    us = [np.tile(u, (m.nelem, 1)) for u in gd.freestream()]
+    us[1][11, 3] = -1.0
+    ud = torch.tensor(np.concatenate(us), device=cuda)
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200, precision=4)
+    rc, st = S.solve(ud, raise_on_error=False)
+    assert rc == fv.FV_ERR_NUMERICAL
+    assert st[1]["status"] == fv.FV_ERR_NUMERICAL
+    assert st[0]["status"] == 0 and st[2]["status"] == 0
+    g0 = fv.FlowFV(m, fv.physics_cfg(**plist[0]), fv.numerics_cfg(flux="ROE"), cases.CHANNEL_BCS)
+    u0 = torch.tensor(np.tile(g0.freestream()[0], (m.nelem, 1)), device=cuda)
+    fv.SteadyBackwardEulerSolver(g0, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200,
+                                 precision=4).solve(u0)
+    a = ud.cpu().numpy()[:m.nelem]
+    assert np.abs(a - u0.cpu().numpy()).max() <= 1e-8 * np.abs(a).max()

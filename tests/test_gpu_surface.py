@@ -55,3 +55,15 @@ def test_surface_data_unknown_marker_rejected(cuda):
     u = torch.tensor(np.tile(gd.freestream()[0], (m.nelem, 1)), device=cuda)
     with pytest.raises(fv.FvensError):
         gd.surface_data(u, 99)
+
+
+@pytest.mark.parametrize("name,mesh,phys,num,bcs", SURFACE_CASES[:2], ids=[c[0] for c in SURFACE_CASES[:2]])
+def test_entropy_error_matches_oracle(cuda, name, mesh, phys, num, bcs):
+    import torch
+    m = mesh()
+    gd = fv.FlowFV(m, fv.physics_cfg(**phys), fv.numerics_cfg(**num), bcs)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), **phys, **num, bcs=bcs)
+    u = cases.perturbed_state(od.freestream(), m.nelem)
+    got = gd.entropy_error(torch.tensor(u, device=cuda))[0]
+    ref = od.entropy_error(u)
+    assert ref > 0 and abs(got - ref) <= 1e-12 * ref

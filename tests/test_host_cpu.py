@@ -95,6 +95,42 @@ def test_gmsh_reader_on_reference_meshes(name):
     _compare_topology(m)
 
 
+REF_TESTCASES = os.path.join(os.path.dirname(REF_MESHES), "..", "testcases") if REF_MESHES else ""
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TESTCASES), reason="reference test cases not present")
+def test_su2_reader_matches_gmsh_twin():
+    """The reference ships the laminar NACA 0012 hybrid mesh in both formats:
+    the SU2 reader (meshreaders.cpp:267-397) must give the same cells,
+    boundary faces and markers as the Gmsh reader."""
+    base = os.path.join(REF_TESTCASES, "visc-naca0012", "grids", "NACA0012_lam_hybrid_1")
+    a = fv.UMesh.read(base + ".su2")
+    b = fv.UMesh.read(base + ".msh")
+    assert (a.nelem, a.nbface, a.npoin) == (b.nelem, b.nbface, b.npoin)
+    ga, gb = a.geometry(), b.geometry()
+    assert abs(ga["area"].sum() - gb["area"].sum()) <= 1e-12 * gb["area"].sum()
+    ea, eb = a.export(), b.export()
+    assert sorted(np.bincount(ea["btag"]).tolist()) == sorted(np.bincount(eb["btag"]).tolist())
+    _compare_topology(a)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TESTCASES), reason="reference test cases not present")
+def test_su2_reader_inviscid_naca_mesh():
+    m = fv.UMesh.read(os.path.join(REF_TESTCASES, "naca0012", "grids", "NACA0012_inv.su2"), reorder=1)
+    e = m.export()
+    assert m.nelem == 10216 and m.npoin == 5233 and m.nbface == 250
+    assert sorted(set(e["btag"].tolist())) == [2, 4]
+    assert m.geometry()["area"].min() > 0
+    _compare_topology(m)
+
+
+def test_mesh_reader_rejects_unknown_extension(tmp_path):
+    p = tmp_path / "mesh.vtu"
+    p.write_text("x")
+    with pytest.raises(fv.FvensError):
+        fv.UMesh.read(str(p))
+
+
 def test_oracle_solves_small_channel():
     m = cases.channel(24, 8)
     od = orc.Disc(orc.Mesh.from_export(m.export()), Minf=0.5, flux="ROE", gradient="LEASTSQUARES",
