@@ -119,7 +119,7 @@ def test_convergence_history_file_format(cuda, tmp_path):
     data = np.genfromtxt(str(path))
     assert data.shape == (st[0]["steps"], 7)
     assert data[0, 0] == 1 and data[-1, 0] == st[0]["steps"]
-    assert data[0, 1] == 0.0 and abs(data[-1, 2] - np.log10(st[0]["res"])) < 1e-5
+    assert data[0, 1] == 0.0 and abs(data[-1, 2] - np.log10(st[0]["res"])) < 1e-4  # 6 significant digits
     assert data[-1, 5] == st[0]["lin_iters"] and data[0, 6] == 10.0
 
 
