@@ -145,3 +145,23 @@ def test_batch_member_failure_is_isolated(cuda):
                                  precision=4).solve(u0)
     a = ud.cpu().numpy()[:m.nelem]
     assert np.abs(a - u0.cpu().numpy()).max() <= 1e-8 * np.abs(a).max()
+
+
+def test_cpp_interface_solves(cuda, tmp_path):
+    """The C++ host interface (include/fvens_gb300.hpp) drives a steady solve
+    through the C ABI with host buffers."""
+    import os
+    import shutil
+    import subprocess
+    from tests.test_host_cpu import CPP_DRIVER, ROOT
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    src = tmp_path / "driver.cpp"
+    src.write_text(CPP_DRIVER)
+    exe = tmp_path / "driver"
+    libdir = os.path.dirname(fv.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-lfvens_gb300", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe), "solve"], check=True, capture_output=True, text=True).stdout.split()
+    steps, res = int(out[3]), float(out[4])
+    assert 0 < steps < 1000 and res <= 1e-10
