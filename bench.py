@@ -276,21 +276,22 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def _timed_solve(torch, S_list, u):
+def _timed_solve(torch, S_list, u, all_members=False):
+    """Runs the solvers in turn on u; (seconds by CUDA events, the last
+    solver's stats of member 0, or of every member)."""
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     ev0.record()
-    sts = [S.solve(u, raise_on_error=False)[1][0] for S in S_list]
+    sts = [S.solve(u, raise_on_error=False)[1] for S in S_list]
     ev1.record()
     torch.cuda.synchronize()
-    return ev0.elapsed_time(ev1) / 1e3, sts[-1]
+    return ev0.elapsed_time(ev1) / 1e3, (sts[-1] if all_members else sts[-1][0])
 
 
 def run_variants(fv, torch, dev, m, main, start, u0d, prec):
-    """The same solve (1) on the plain path: FP64 Jacobian and FP64 ILU(0),
-    freestream start; (2) on the FP32 path warm-started from the converged
-    state of a neighbouring condition (M 0.79), without the starter.  One
-    timed solve each (CUDA events)."""
+    """(1) The same solve on the plain path: FP64 Jacobian and FP64 ILU(0),
+    freestream start, one timed solve (CUDA events).  (2) Batched laminar
+    solves (run_batched)."""
     out = {}
     u = torch.empty_like(u0d)
     P1 = fv.SteadyBackwardEulerSolver(start, precision=8, **STARTER)
@@ -300,19 +301,39 @@ def run_variants(fv, torch, dev, m, main, start, u0d, prec):
     out["plain_fp64_cold"] = {"solves_s": 1.0 / t, "s_per_solve": t, "main_steps": st["steps"],
                               "linear_iters": st["lin_iters"], "converged": st["status"] == 0, "res": st["res"]}
     del P1, P2
-    ph_nb = fv.physics_cfg(**dict(PHYS, Minf=PHYS["Minf"] - 0.01))
-    main_nb = fv.FlowFV(m, ph_nb, fv.numerics_cfg(**NUM_MAIN), BCS)
-    start_nb = fv.FlowFV(m, ph_nb, fv.numerics_cfg(**NUM_START), BCS)
-    u_nb = torch.tensor(np.tile(main_nb.freestream()[0], (m.nelem, 1)), device=dev)
-    fv.SteadyBackwardEulerSolver(start_nb, precision=prec, **STARTER).solve(u_nb, raise_on_error=False)
-    fv.SteadyBackwardEulerSolver(main_nb, precision=prec, **MAIN).solve(u_nb, raise_on_error=False)
-    W = fv.SteadyBackwardEulerSolver(main, precision=prec, **MAIN)
-    u.copy_(u_nb)
-    t, st = _timed_solve(torch, [W], u)
-    out["fp32_warm_from_M0.79"] = {"solves_s": 1.0 / t, "s_per_solve": t, "main_steps": st["steps"],
-                                   "linear_iters": st["lin_iters"], "converged": st["status"] == 0,
-                                   "res": st["res"]}
+    out["batched_laminar"] = run_batched(fv, torch, dev)
     return out
+
+
+def run_batched(fv, torch, dev, B=64, seed=7):
+    """Batched solves of B laminar conditions (M ~ U[0.3, 0.7], AoA ~ U[-4, 4] deg,
+    Re ~ U[2000, 10000], Pr 0.72, adiabatic wall; Roe, least squares) on the
+    reference's hybrid NACA 0012 mesh (13,156 cells), all members in the same
+    launches, against one member alone."""
+    import collections
+    z = np.load(os.path.join(ROOT, "tests", "golden", "naca0012_lam_hybrid_1_mesh.npz"))
+    m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
+                             z["btag"].astype(np.int32), reorder=1)
+    bcs = [(4, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))]
+    rng = np.random.default_rng(seed)
+    M, A, Re = rng.uniform(0.3, 0.7, B), rng.uniform(-4, 4, B), rng.uniform(2000, 10000, B)
+    phs = [fv.physics_cfg(Minf=float(M[k]), aoa_deg=float(A[k]), Reinf=float(Re[k]), Tinf=288.15, Pr=0.72,
+                          viscous=True) for k in range(B)]
+    res = {"mesh_cells": m.nelem, "batch": B}
+    for tag, plist in (("single", phs[:1]), ("batch", phs)):
+        start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), bcs)
+        main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), bcs)
+        u = torch.tensor(np.concatenate([np.tile(x, (m.nelem, 1)) for x in main.freestream()]), device=dev)
+        S1 = fv.SteadyBackwardEulerSolver(start, cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0,
+                                          max_timesteps=50, pc="ilu0", nl_update=2, precision=4)
+        S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=500, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
+                                          max_timesteps=600, pc="ilu0", nl_update=2, precision=4)
+        t, stats = _timed_solve(torch, [S1, S2], u, all_members=True)
+        conv = sum(1 for st in stats if st["status"] == 0)
+        res[tag] = {"seconds": t, "converged": conv, "members": len(plist), "converged_solves_s": conv / t,
+                    "status_counts": dict(collections.Counter(int(st["status"]) for st in stats)),
+                    "main_steps_max": max(st["steps"] for st in stats)}
+    return res
 
 
 def _oracle_case(m):
