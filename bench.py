@@ -115,15 +115,14 @@ def run_ours(args):
 
     import fvens_gb300 as fv
     from fvens_gb300 import build as fvbuild
+    from fvens_gb300.replicas import Replicas
 
     rank, world, local = _dist()
     if not os.path.exists(fv.LIB_PATH):
         fvbuild.build_library()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
+    reps = Replicas("nccl", dev)
     m, main, start = build_case(fv)
     prec = 8 if args.plain else 4
     S1 = fv.SteadyBackwardEulerSolver(start, precision=prec, **STARTER)
@@ -143,10 +142,7 @@ def run_ours(args):
             torch.cuda.nvtx.range_pop()
         return st1[0], st2[0]
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    barrier = reps.barrier
 
     for _ in range(args.warmup):
         solve_device()
@@ -165,12 +161,8 @@ def run_ours(args):
     barrier()
     ms = ev0.elapsed_time(ev1)
     launches = fv.kernel_launch_count() - launches0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms / 1e3)
+    value = reps.throughput(args.steps, ms / 1e3)
+    ms = reps.max_over_ranks(ms)
     converged = all(s2["status"] == 0 for _, s2 in stats)
 
     # end to end through the host-buffer C-ABI call: pinned host state in,
@@ -185,13 +177,7 @@ def run_ours(args):
         S1.solve_host(hn, raise_on_error=False)
         S2.solve_host(hn, raise_on_error=False)
     t1 = time.perf_counter()
-    e2e_s = t1 - t0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * args.steps / e2e_s
+    e2e_value = reps.throughput(args.steps, t1 - t0)
     cl = main.surface_data(ud, 2)[0]
     u_conv = ud.clone()
     variants = {} if args.no_variants else run_variants(fv, torch, dev, m, main, start, u0d, prec)
@@ -271,9 +257,7 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(m, s1, s2, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    reps.close()
 
 
 def _timed_solve(torch, S_list, u, all_members=False):
