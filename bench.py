@@ -131,6 +131,8 @@ def run_ours(args):
     u0 = np.ascontiguousarray(np.tile(uinf, (m.nelem, 1)))
     ud = torch.empty((m.nelem, 4), dtype=torch.float64, device=dev)
     u0d = torch.tensor(u0, device=dev)
+    # launch geometry of the residual kernels picked by the autotuner (untimed)
+    block_sizes = {"main": main.autotune(u0d), "starter": start.autotune(u0d)}
 
     def solve_device():
         ud.copy_(u0d)
@@ -236,7 +238,8 @@ def run_ours(args):
                    "l2": "working set > L2 (no flush needed)",
                    "starter_steps": s1["steps"], "main_steps": steps_main, "linear_iters": lin_main,
                    "converged": converged, "final_res": s2["res"],
-                   "cl_cdp": [float(cl[0]), float(cl[1])]},
+                   "cl_cdp": [float(cl[0]), float(cl[1])],
+                   "residual_block_sizes": block_sizes},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(u0.nbytes),
                 "d2h_bytes_per_step": int(u0.nbytes)},
         "gpu_launches": int(launches),

@@ -254,6 +254,13 @@ class FlowFV:
             check(rc)
         return rc, steps, tm
 
+    def autotune(self, u):
+        """Picks the residual kernels' block sizes by timing them at state u
+        (fv_disc_autotune); returns [states, gradients, faces, gather]."""
+        bs = np.zeros(4, np.int32)
+        check(lib().fv_disc_autotune(self._h, _vp(dptr(u)), _hp(bs, ctypes.c_int)))
+        return bs.tolist()
+
     def entropy_error(self, u):
         """FlowOutput::compute_entropy_cell per batch member."""
         out = np.zeros(self.batch)

@@ -384,6 +384,15 @@ fv_status fv_compute_residual(fv_disc *D, const double *u, double *r, int gettim
 	return cuda_status(e, "residual");
 }
 
+fv_status fv_disc_autotune(fv_disc *D, const double *u, int *h_block_sizes)
+{
+	if (!D || !u) { set_error("null argument"); return FV_ERR_INVALID; }
+	const int before = D->kernels_launched;
+	const cudaError_t e = residual_autotune(D, u, D->stream, h_block_sizes);
+	count_launches(D->kernels_launched - before);
+	return cuda_status(e, "autotune");
+}
+
 fv_status fv_get_gradients(fv_disc *D, const double *u, double *grad, int primitive)
 {
 	if (!D || !u || !grad) { set_error("null argument"); return FV_ERR_INVALID; }

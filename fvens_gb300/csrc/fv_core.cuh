@@ -95,6 +95,8 @@ struct ResidualWork {
 	double2 *spec = nullptr;   // [batch][naface] spectral radii (left, right)
 };
 
+enum { KBS_PREP = 0, KBS_GRAD = 1, KBS_FACE = 2, KBS_GATHER = 3 };
+
 struct fv_disc_impl {
 	fv_mesh_impl *mesh = nullptr;
 	DiscDev d;
@@ -105,6 +107,7 @@ struct fv_disc_impl {
 	// owned device arrays
 	std::vector<void *> owned;
 	ResidualWork w;
+	int bs[4] = {128, 128, 128, 128};  // block sizes of the residual kernels (KBS_*), fv_disc_autotune
 	int *btag = nullptr;       // device: boundary marker of each boundary face
 	double *surf = nullptr;    // device: surface-integral partials [batch][4]
 	cudaStream_t stream = 0;
@@ -118,6 +121,9 @@ cudaError_t gradients_launch(fv_disc_impl *D, const double *u, double *grad, int
 /* the residual's passes before the face kernel (primitive/ghost states,
  * gradients, limiter values, WENO blend) into the handle's scratch */
 cudaError_t gradient_pass_launch(fv_disc_impl *D, const double *u, cudaStream_t s);
+/* times the residual kernels at 64 / 128 / 256 threads per block at state u
+ * and keeps the fastest per kernel in D->bs; chosen[4] (may be NULL) receives them */
+cudaError_t residual_autotune(fv_disc_impl *D, const double *u, cudaStream_t s, int *chosen);
 /* the face-flux launch alone (reads the prep/gradient/limiter results of the
  * last residual evaluation of the same state) */
 cudaError_t face_launch(fv_disc_impl *D, const double *u, int gettimesteps, cudaStream_t s);

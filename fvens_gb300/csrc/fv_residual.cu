@@ -18,77 +18,84 @@ namespace fvg {
 
 namespace {
 
-constexpr int BS = 128;
+// block sizes are chosen per discretisation at run time (fv_disc_autotune);
+// kMaxBS bounds them for register allocation
+constexpr int kMaxBS = 256;
 
-__global__ void __launch_bounds__(BS) k_prep(DiscDev D, const double *__restrict__ u, ResidualWork w)
+__global__ void __launch_bounds__(kMaxBS) k_prep(DiscDev D, const double *__restrict__ u, ResidualWork w)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
-	prep_body(D, b, blockIdx.x * BS + threadIdx.x, u, w);
+	prep_body(D, b, blockIdx.x * blockDim.x + threadIdx.x, u, w);
 }
 
-__global__ void __launch_bounds__(BS) k_grad(DiscDev D, const d4 *__restrict__ q, const d4 *__restrict__ qg,
-                                             d4 *__restrict__ grad, d4 *__restrict__ phi, int limiter)
+__global__ void __launch_bounds__(kMaxBS) k_grad(DiscDev D, const d4 *__restrict__ q, const d4 *__restrict__ qg,
+                                                 d4 *__restrict__ grad, d4 *__restrict__ phi, int limiter)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
-	const int i = blockIdx.x * BS + threadIdx.x;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= D.nelem) return;
 	grad_body(D, b, i, q, qg, grad, phi, limiter);
 }
 
-__global__ void __launch_bounds__(BS) k_weno(DiscDev D, const d4 *__restrict__ grad, d4 *__restrict__ lgrad)
+__global__ void __launch_bounds__(kMaxBS) k_weno(DiscDev D, const d4 *__restrict__ grad, d4 *__restrict__ lgrad)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
-	const int i = blockIdx.x * BS + threadIdx.x;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= D.nelem) return;
 	weno_body(D, b, i, grad, lgrad);
 }
 
 template <int FLUX, int VISC>
-__global__ void __launch_bounds__(BS) k_face(DiscDev D, const double *__restrict__ u, ResidualWork w, int getdt)
+__global__ void __launch_bounds__(kMaxBS) k_face(DiscDev D, const double *__restrict__ u, ResidualWork w, int getdt)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
-	const int f = blockIdx.x * BS + threadIdx.x;
+	const int f = blockIdx.x * blockDim.x + threadIdx.x;
 	if (f >= D.naface) return;
 	face_body<FLUX, VISC>(D, b, f, u, w, getdt);
 }
 
-__global__ void __launch_bounds__(BS) k_gather(DiscDev D, ResidualWork w, double *__restrict__ r, double *__restrict__ dt)
+__global__ void __launch_bounds__(kMaxBS) k_gather(DiscDev D, ResidualWork w, double *__restrict__ r,
+                                                   double *__restrict__ dt)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
-	const int i = blockIdx.x * BS + threadIdx.x;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= D.nelem) return;
 	gather_body(D, b, i, w, r, dt);
 }
 
 template <int FLUX>
-void launch_face(fv_disc_impl *Dh, const double *u, int getdt, dim3 grid, cudaStream_t s)
+void launch_face(fv_disc_impl *Dh, const double *u, int getdt, dim3 grid, int bs, cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
 	const int visc = !D.viscous ? 0 : (D.constvisc ? 2 : 1);
-	if (visc == 0) k_face<FLUX, 0><<<grid, BS, 0, s>>>(D, u, Dh->w, getdt);
-	else if (visc == 1) k_face<FLUX, 1><<<grid, BS, 0, s>>>(D, u, Dh->w, getdt);
-	else k_face<FLUX, 2><<<grid, BS, 0, s>>>(D, u, Dh->w, getdt);
+	if (visc == 0) k_face<FLUX, 0><<<grid, bs, 0, s>>>(D, u, Dh->w, getdt);
+	else if (visc == 1) k_face<FLUX, 1><<<grid, bs, 0, s>>>(D, u, Dh->w, getdt);
+	else k_face<FLUX, 2><<<grid, bs, 0, s>>>(D, u, Dh->w, getdt);
 }
+
+/* grid of n items in blocks of bs, one row per batch member */
+dim3 grid_of(int n, int bs, int batch) { return dim3((unsigned)((n + bs - 1) / bs), (unsigned)batch); }
 
 }  // namespace
 
 cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
-	const dim3 gf((unsigned)((D.naface + BS - 1) / BS), (unsigned)Dh->batch);
+	const int bs = Dh->bs[KBS_FACE];
+	const dim3 gf = grid_of(D.naface, bs, Dh->batch);
 	switch (D.flux) {
-	case FLUX_LLF: launch_face<FLUX_LLF>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_VANLEER: launch_face<FLUX_VANLEER>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_AUSM: launch_face<FLUX_AUSM>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_AUSMPLUS: launch_face<FLUX_AUSMPLUS>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_ROE: launch_face<FLUX_ROE>(Dh, u, gettimesteps, gf, s); break;
-	case FLUX_HLL: launch_face<FLUX_HLL>(Dh, u, gettimesteps, gf, s); break;
-	default: launch_face<FLUX_HLLC>(Dh, u, gettimesteps, gf, s); break;
+	case FLUX_LLF: launch_face<FLUX_LLF>(Dh, u, gettimesteps, gf, bs, s); break;
+	case FLUX_VANLEER: launch_face<FLUX_VANLEER>(Dh, u, gettimesteps, gf, bs, s); break;
+	case FLUX_AUSM: launch_face<FLUX_AUSM>(Dh, u, gettimesteps, gf, bs, s); break;
+	case FLUX_AUSMPLUS: launch_face<FLUX_AUSMPLUS>(Dh, u, gettimesteps, gf, bs, s); break;
+	case FLUX_ROE: launch_face<FLUX_ROE>(Dh, u, gettimesteps, gf, bs, s); break;
+	case FLUX_HLL: launch_face<FLUX_HLL>(Dh, u, gettimesteps, gf, bs, s); break;
+	default: launch_face<FLUX_HLLC>(Dh, u, gettimesteps, gf, bs, s); break;
 	}
 	return cudaGetLastError();
 }
@@ -99,16 +106,16 @@ cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t
 {
 	const DiscDev &D = Dh->d;
 	const int B = Dh->batch;
-	auto grid = [&](int n) { return dim3((unsigned)((n + BS - 1) / BS), (unsigned)B); };
+	const int bp = Dh->bs[KBS_PREP], bg = Dh->bs[KBS_GRAD];
 	int nk = 0;
-	k_prep<<<grid(D.nelem + D.nbface), BS, 0, s>>>(D, u, Dh->w);
+	k_prep<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, Dh->w);
 	nk++;
 	if (D.gradscheme != GRAD_NONE) {
 		const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
-		k_grad<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, lim);
+		k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, lim);
 		nk++;
 		if (D.recon == REC_WENO) {
-			k_weno<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.grad, Dh->w.lgrad);
+			k_weno<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, Dh->w.grad, Dh->w.lgrad);
 			nk++;
 		}
 	} else {
@@ -116,7 +123,7 @@ cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t
 		if (D.recon == REC_WENO) cudaMemsetAsync(Dh->w.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
 		if (D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN) {
 			// zero gradients: every face value equals the cell value, the limiter is 1
-			k_grad<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, 0);
+			k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, 0);
 			nk++;
 		}
 	}
@@ -127,13 +134,13 @@ cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t
 cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int gettimesteps, double *dt, cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
-	auto grid = [&](int n) { return dim3((unsigned)((n + BS - 1) / BS), (unsigned)Dh->batch); };
 	if (D.order2) {
 		const cudaError_t e = gradient_pass_launch(Dh, u, s);
 		if (e) return e;
 	}
 	face_launch(Dh, u, gettimesteps, s);
-	k_gather<<<grid(D.nelem), BS, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
+	const int bc = Dh->bs[KBS_GATHER];
+	k_gather<<<grid_of(D.nelem, bc, Dh->batch), bc, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
 	Dh->kernels_launched += 2;
 	return cudaGetLastError();
 }
@@ -145,7 +152,8 @@ cudaError_t gradients_launch(fv_disc_impl *Dh, const double *u, double *grad, in
 {
 	const DiscDev &D = Dh->d;
 	const int B = Dh->batch;
-	auto grid = [&](int n) { return dim3((unsigned)((n + BS - 1) / BS), (unsigned)B); };
+	auto grid = [&](int n) { return grid_of(n, 128, B); };
+	constexpr int BS = 128;
 	k_prep<<<grid(D.nelem + D.nbface), BS, 0, s>>>(D, u, Dh->w);
 	const d4 *q = conserved ? reinterpret_cast<const d4 *>(u) : Dh->w.prim;
 	const d4 *qg = conserved ? Dh->w.ghost_cons : Dh->w.ghost_prim;
@@ -157,6 +165,62 @@ cudaError_t gradients_launch(fv_disc_impl *Dh, const double *u, double *grad, in
 		Dh->kernels_launched += 2;
 	}
 	return cudaGetLastError();
+}
+
+}  // namespace fvg
+
+namespace fvg {
+
+/* Launch-geometry autotuner of the residual kernels: each kernel runs with
+ * 64, 128 and 256 threads per block at state u (one warm-up, then three timed
+ * launches with CUDA events) and keeps the fastest.  Every thread does the work
+ * of one cell or face whatever the block size, so the choice changes timing,
+ * not results. */
+cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s, int *chosen)
+{
+	const DiscDev &D = Dh->d;
+	const int B = Dh->batch;
+	const int cand[3] = {64, 128, 256};
+	double *r = nullptr;
+	cudaError_t e = cudaMalloc(&r, sizeof(double) * 4 * (size_t)D.nelem * B);
+	if (!e) e = gradient_pass_launch(Dh, u, s);  // fill the scratch the later kernels read
+	cudaEvent_t a, b;
+	cudaEventCreate(&a);
+	cudaEventCreate(&b);
+	const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
+	auto launch = [&](int kind, int bs) {
+		switch (kind) {
+		case KBS_PREP: k_prep<<<grid_of(D.nelem + D.nbface, bs, B), bs, 0, s>>>(D, u, Dh->w); break;
+		case KBS_GRAD:
+			if (D.order2) k_grad<<<grid_of(D.nelem, bs, B), bs, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad,
+			                                                              Dh->w.phi, lim);
+			break;
+		case KBS_FACE: Dh->bs[KBS_FACE] = bs; face_launch(Dh, u, 1, s); break;
+		default: k_gather<<<grid_of(D.nelem, bs, B), bs, 0, s>>>(D, Dh->w, r, nullptr); break;
+		}
+		return cudaGetLastError();
+	};
+	for (int kind = 0; kind < 4 && !e; kind++) {
+		float best = 1e30f;
+		int pick = Dh->bs[kind];
+		for (int c = 0; c < 3 && !e; c++) {
+			e = launch(kind, cand[c]);
+			if (!e) e = cudaEventRecord(a, s);
+			for (int k = 0; k < 3 && !e; k++) e = launch(kind, cand[c]);
+			if (!e) e = cudaEventRecord(b, s);
+			if (!e) e = cudaEventSynchronize(b);
+			float ms = 0;
+			if (!e) e = cudaEventElapsedTime(&ms, a, b);
+			if (!e && ms < best) { best = ms; pick = cand[c]; }
+		}
+		Dh->bs[kind] = pick;
+		if (chosen) chosen[kind] = pick;
+	}
+	Dh->kernels_launched += 4 * 3 * 4 + 2;
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	if (r) cudaFree(r);
+	return e;
 }
 
 }  // namespace fvg

@@ -110,3 +110,20 @@ def test_freestream_is_steady(cuda):
     rd = torch.zeros_like(ud)
     gd.compute_residual(ud, rd, False, None)
     assert np.abs(rd.cpu().numpy()).max() < 1e-12
+
+
+def test_autotune_keeps_results(cuda):
+    """The residual kernels' block sizes picked by fv_disc_autotune change
+    timing only: the residual and local time steps are bitwise unchanged."""
+    import torch
+    name, mesh, phys, num, bcs = cases.RESIDUAL_CASES[1]
+    m = mesh()
+    gd = fv.FlowFV(m, fv.physics_cfg(**phys), fv.numerics_cfg(**num), bcs)
+    u = torch.tensor(cases.perturbed_state(gd.freestream()[0], m.nelem), device=cuda)
+    r0, dt0 = torch.zeros_like(u), torch.zeros(m.nelem, dtype=torch.float64, device=cuda)
+    gd.compute_residual(u, r0, True, dt0)
+    bs = gd.autotune(u)
+    assert len(bs) == 4 and all(b in (64, 128, 256) for b in bs)
+    r1, dt1 = torch.zeros_like(u), torch.zeros_like(dt0)
+    gd.compute_residual(u, r1, True, dt1)
+    assert torch.equal(r0, r1) and torch.equal(dt0, dt1)
