@@ -213,6 +213,15 @@ fv_status fv_mesh_read(const char *path, int reorder, fv_mesh **out)
 	return FV_ERR_INVALID;
 }
 
+fv_status fv_mesh_periodic_map(const fv_mesh *m, int marker, int axis, int *map)
+{
+	if (!m || !map) { set_error("null argument"); return FV_ERR_INVALID; }
+	if (axis < 0 || axis > 1) { set_error("periodic axis must be 0 or 1"); return FV_ERR_INVALID; }
+	const std::vector<int> pm = periodic_map(m->h, marker, axis);
+	std::copy(pm.begin(), pm.end(), map);
+	return FV_OK;
+}
+
 fv_status fv_mesh_counts(const fv_mesh *m, int c[6])
 {
 	if (!m || !c) { set_error("null argument"); return FV_ERR_INVALID; }

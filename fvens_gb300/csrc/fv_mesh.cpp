@@ -675,6 +675,27 @@ int read_gmsh2(const std::string &path, RawMesh &out, std::string *err)
 
 namespace fvg {
 
+std::vector<int> periodic_map(const HostMesh &h, int bcm, int axis)
+{
+	std::vector<int> map(h.nbface, -1);
+	if (bcm < 0 || axis < 0 || axis > 1) return map;
+	const int ax = 1 - axis;
+	auto centre = [&](int f) { return (h.coords[2 * h.bface[2 * f] + ax] + h.coords[2 * h.bface[2 * f + 1] + ax]) / 2.0; };
+	for (int i = 0; i < h.nbface; i++) {
+		if (h.btag[i] != bcm || map[i] > -1) continue;
+		const double ci = centre(i);
+		for (int j = i + 1; j < h.nbface; j++) {
+			if (h.btag[j] != bcm || map[j] > -1) continue;
+			if (std::fabs(ci - centre(j)) <= 1e-8) {
+				map[i] = j;
+				map[j] = i;
+				break;
+			}
+		}
+	}
+	return map;
+}
+
 BlockOrder block_colour_order(const HostMesh &h, int part_size)
 {
 	BlockOrder o;

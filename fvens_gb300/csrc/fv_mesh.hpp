@@ -71,6 +71,12 @@ struct BlockOrder {
 };
 BlockOrder block_colour_order(const HostMesh &h, int part_size);
 
+/* Periodic pairing of the boundary faces of marker bcm (UMesh::compute_periodic_map,
+ * mesh.cpp:368-421): two faces pair when their centres' coordinate along the
+ * axis other than `axis` agrees to 1e-8, the first unpaired later face
+ * winning.  map[f] = partner face (boundary-face index) or -1. */
+std::vector<int> periodic_map(const HostMesh &h, int bcm, int axis);
+
 /* Reverse Cuthill-McKee ordering of the cell graph (own implementation:
  * George-Liu pseudo-peripheral start, neighbours visited by increasing degree). */
 std::vector<int> rcm_order(int n, const std::vector<int> &adj_ptr, const std::vector<int> &adj);

@@ -120,6 +120,12 @@ fv_status fv_mesh_geometry(const fv_mesh *m, int *face_lr, double *fnorm, double
 /* block-colour elimination order of the SGS / ILU(0) preconditioners
  * (compact parts of ~part_size cells, parts coloured): order[position] = cell */
 fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *nparts, int *ncolors);
+/* UMesh::compute_periodic_map (mesh.cpp:368-421): pairs the boundary faces of
+ * `marker` whose centres agree (to 1e-8) along the axis other than `axis`
+ * (0 = x, 1 = y); map[nbface] = partner boundary face or -1.  The flow
+ * discretisation, as the reference's, has no periodic boundary condition
+ * (FV_BC_PERIODIC is rejected). */
+fv_status fv_mesh_periodic_map(const fv_mesh *m, int marker, int axis, int *map);
 void fv_mesh_destroy(fv_mesh *m);
 
 /* ---- spatial discretisation: FlowFV<freal,order2,constVisc> (afactory.cpp:252-276) ---- */

@@ -209,3 +209,17 @@ def test_cpp_interface_builds_and_links(tmp_path):
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     m = fv.UMesh.generate(fv.MESH_CHANNEL_BUMP, [24, 8, 0.5, 1])
     assert [int(x) for x in out[:3]] == [m.nelem, m.nbface, m.naface]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference test meshes not present")
+def test_periodic_map_on_reference_mesh():
+    """tests/mesh/mesh.cpp:test_periodic_map: on testperiodic.msh, marker 4,
+    axis 0, boundary faces 8..12 pair with 25..21."""
+    import ctypes
+    m = fv.UMesh.read_gmsh(os.path.join(REF_MESHES, "testperiodic.msh"))
+    pm = np.zeros(m.nbface, np.int32)
+    fv.check(fv.lib().fv_mesh_periodic_map(m._h, 4, 0, fv._hp(pm, ctypes.c_int)))
+    for a, b in zip([8, 9, 10, 11, 12], [25, 24, 23, 22, 21]):
+        assert pm[a] == b and pm[b] == a
+    e = m.export()
+    assert np.all(pm[e["btag"] != 4] == -1)
