@@ -149,6 +149,15 @@ class UMesh:
         check(lib().fv_mesh_read(path.encode(), int(reorder), ctypes.byref(h)))
         return cls(h)
 
+    def find_lines(self, threshold):
+        """Lines of strongly coupled cells (the reference's findLines); the mesh
+        keeps them for preconditioners created afterwards.  Returns
+        (number of lines, line index of every cell or -1)."""
+        cl = np.zeros(self.nelem, np.int32)
+        nl = ctypes.c_int()
+        check(lib().fv_mesh_find_lines(self._h, ctypes.c_double(threshold), ctypes.byref(nl), _hp(cl, ctypes.c_int)))
+        return nl.value, cl
+
     def export(self):
         coords = np.zeros((self.npoin, 2))
         nnode = np.zeros(self.nelem, np.int32)

@@ -213,6 +213,19 @@ fv_status fv_mesh_read(const char *path, int reorder, fv_mesh **out)
 	return FV_ERR_INVALID;
 }
 
+fv_status fv_mesh_find_lines(fv_mesh *m, double threshold, int *nlines, int *cell_line)
+{
+	if (!m) { set_error("null argument"); return FV_ERR_INVALID; }
+	const int nl = threshold > 0 ? find_lines(m->h, threshold) : 0;
+	if (threshold <= 0) {
+		m->h.lines.clear();
+		m->h.cell_line.assign(m->h.nelem, -1);
+	}
+	if (nlines) *nlines = nl;
+	if (cell_line) std::copy(m->h.cell_line.begin(), m->h.cell_line.end(), cell_line);
+	return FV_OK;
+}
+
 fv_status fv_mesh_periodic_map(const fv_mesh *m, int marker, int axis, int *map)
 {
 	if (!m || !map) { set_error("null argument"); return FV_ERR_INVALID; }

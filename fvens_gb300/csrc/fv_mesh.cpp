@@ -2,6 +2,7 @@
 #include "fv_mesh.hpp"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -675,6 +676,53 @@ int read_gmsh2(const std::string &path, RawMesh &out, std::string *err)
 
 namespace fvg {
 
+int find_lines(HostMesh &h, double threshold)
+{
+	const int n = h.nelem;
+	// neighbours of each cell ordered by decreasing weight (computeWeights)
+	std::vector<std::array<std::pair<double, int>, 4>> w(n);
+	std::vector<int> nreal(n, 0);
+	for (int i = 0; i < n; i++) {
+		double minw = 1e20;
+		int k = 0;
+		for (int j = 0; j < h.nnode[i]; j++) {
+			const int nb = h.esuel[4 * i + j];
+			if (nb < 0) continue;
+			const double dx = h.cc[2 * i] - h.cc[2 * nb], dy = h.cc[2 * i + 1] - h.cc[2 * nb + 1];
+			const double wt = 1.0 / std::sqrt(dx * dx + dy * dy);
+			if (wt < minw) minw = wt;
+			w[i][k++] = {wt, nb};
+		}
+		for (int a = 0; a < k; a++) w[i][a].first /= minw;
+		std::stable_sort(w[i].begin(), w[i].begin() + k,
+		                 [](const std::pair<double, int> &a, const std::pair<double, int> &b) { return a.first > b.first; });
+		nreal[i] = k;
+	}
+	h.lines.clear();
+	h.cell_line.assign(n, -1);
+	for (int f = 0; f < h.nbface; f++) {
+		const int b = h.face_l[f];
+		if (h.cell_line[b] >= 0) continue;
+		std::vector<int> line;
+		int cur = b;
+		while (true) {
+			if (nreal[cur] == 0 || !(w[cur][0].first > threshold)) break;
+			line.push_back(cur);
+			h.cell_line[cur] = (int)h.lines.size();
+			int next = -1;
+			for (int j = 0; j < nreal[cur]; j++) {
+				const int nb = w[cur][j].second;
+				if (h.cell_line[nb] == -1 && w[cur][j].first > threshold) { next = nb; break; }
+			}
+			if (next < 0) break;
+			cur = next;
+		}
+		if (line.size() > 1) h.lines.push_back(line);
+		else if (line.size() == 1) h.cell_line[line[0]] = -1;
+	}
+	return (int)h.lines.size();
+}
+
 std::vector<int> periodic_map(const HostMesh &h, int bcm, int axis)
 {
 	std::vector<int> map(h.nbface, -1);
@@ -704,24 +752,40 @@ BlockOrder block_colour_order(const HostMesh &h, int part_size)
 	// parts grown breadth-first over the cell graph, each from the lowest-numbered
 	// cell not yet in a part: compact in the cell graph, so the dependency chains
 	// inside a part are about as long as the part is wide (in cells)
+	// units that go into a part whole: a single cell, or a piece (at most
+	// `target` cells) of a line of strongly coupled cells
+	std::vector<int> unit_of(n, -1);
+	std::vector<std::vector<int>> units;
+	for (const auto &ln : h.lines)
+		for (size_t a = 0; a < ln.size(); a += target) {
+			units.emplace_back(ln.begin() + a, ln.begin() + std::min(ln.size(), a + target));
+			for (int c : units.back()) unit_of[c] = (int)units.size() - 1;
+		}
+	for (int c = 0; c < n; c++)
+		if (unit_of[c] < 0) {
+			unit_of[c] = (int)units.size();
+			units.push_back({c});
+		}
 	std::vector<int> pid(n, -1);
 	std::vector<std::vector<int>> cells;
 	std::vector<int> queue;
 	queue.reserve(target);
+	auto add_unit = [&](int u, int k) {
+		for (int c : units[u]) {
+			pid[c] = k;
+			queue.push_back(c);
+		}
+	};
 	for (int seed = 0; seed < n; seed++) {
 		if (pid[seed] >= 0) continue;
 		const int k = (int)cells.size();
 		queue.clear();
-		queue.push_back(seed);
-		pid[seed] = k;
+		add_unit(unit_of[seed], k);
 		for (size_t head = 0; head < queue.size() && queue.size() < target; head++) {
 			const int c = queue[head];
 			for (int j = 0; j < h.nnode[c] && queue.size() < target; j++) {
 				const int nb = h.esuel[4 * c + j];
-				if (nb >= 0 && pid[nb] < 0) {
-					pid[nb] = k;
-					queue.push_back(nb);
-				}
+				if (nb >= 0 && pid[nb] < 0 && queue.size() + units[unit_of[nb]].size() <= target) add_unit(unit_of[nb], k);
 			}
 		}
 		cells.push_back(queue);

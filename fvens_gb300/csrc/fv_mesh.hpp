@@ -42,6 +42,9 @@ struct HostMesh {
 	int ncolors = 0;
 	std::vector<int> color;               // nelem
 	std::vector<int> color_ptr, color_cells;
+	// lines of strongly coupled cells (find_lines); empty unless requested
+	std::vector<std::vector<int>> lines;
+	std::vector<int> cell_line;           // nelem: line of the cell or -1
 
 	int build(std::string *err);          // topology + geometry + colouring
 	int check(std::string *err) const;    // positive areas, closed cells
@@ -55,7 +58,10 @@ int mesh_from_arrays(HostMesh &m, int npoin, const double *coords, int nelem, co
 /* Block-colour elimination order for the SGS / ILU(0) preconditioners:
  * cells are split into parts of at most part_size cells grown breadth-first
  * over the cell graph (each from the lowest-numbered free cell), parts sharing a face get different
- * colours, and the order is colour-major, then part-major, then inside a part
+ * colours (when the mesh has lines, find_lines, a part takes whole lines --
+ * lines longer than a part in consecutive pieces -- so that the strong
+ * couplings along a line are eliminated inside one part), and the order is
+ * colour-major, then part-major, then inside a part
  * by dependency level (ties by cell index).  Within a part the relative order
  * of any two adjacent cells is their index order, so ILU(0) on this order
  * equals ILU(0) on the cell order with the couplings between same-colour parts
@@ -70,6 +76,15 @@ struct BlockOrder {
 	std::vector<int> lev_pos;    // level start positions (each part's levels in order)
 };
 BlockOrder block_colour_order(const HostMesh &h, int part_size);
+
+/* Lines of strongly coupled cells (findLines / computeWeights,
+ * meshordering.cpp:131-262): the weight of a cell's interior neighbour is
+ * (1/centroid distance) over the smallest such value about the cell; from the
+ * cell of each physical boundary face (in boundary-face order) a line follows
+ * the strongest-weighted neighbour not yet in a line while that weight exceeds
+ * threshold; lines of one cell are dropped.  Stores h.lines, h.cell_line and
+ * returns the number of lines. */
+int find_lines(HostMesh &h, double threshold);
 
 /* Periodic pairing of the boundary faces of marker bcm (UMesh::compute_periodic_map,
  * mesh.cpp:368-421): two faces pair when their centres' coordinate along the

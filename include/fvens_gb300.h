@@ -120,6 +120,14 @@ fv_status fv_mesh_geometry(const fv_mesh *m, int *face_lr, double *fnorm, double
 /* block-colour elimination order of the SGS / ILU(0) preconditioners
  * (compact parts of ~part_size cells, parts coloured): order[position] = cell */
 fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *nparts, int *ncolors);
+/* Lines of strongly coupled cells (findLines, meshordering.cpp:131-262; the
+ * reference's -mesh_reorder line -mesh_anisotropy_threshold): from the cell
+ * of each boundary face, follow the neighbour of largest (1/distance) weight,
+ * relative to the cell's smallest, while it exceeds threshold.  The mesh keeps
+ * the lines: preconditioners created afterwards put whole lines into their
+ * parts.  threshold <= 0 removes them.  *nlines, cell_line[nelem] (line index
+ * or -1; either may be NULL) receive the result. */
+fv_status fv_mesh_find_lines(fv_mesh *m, double threshold, int *nlines, int *cell_line);
 /* UMesh::compute_periodic_map (mesh.cpp:368-421): pairs the boundary faces of
  * `marker` whose centres agree (to 1e-8) along the axis other than `axis`
  * (0 = x, 1 = y); map[nbface] = partner boundary face or -1.  The flow

@@ -223,3 +223,34 @@ def test_periodic_map_on_reference_mesh():
         assert pm[a] == b and pm[b] == a
     e = m.export()
     assert np.all(pm[e["btag"] != 4] == -1)
+
+
+def test_find_lines_on_boundary_layer_mesh():
+    """findLines (meshordering.cpp:208-262) on the reference's laminar hybrid
+    mesh: lines start at boundary cells, follow face neighbours, and every
+    step's weight (1/distance over the cell's smallest) exceeds the threshold."""
+    from tests import regression_cases as rc
+    m, c, regr = rc.load("laminar_naca0012_hybrid1")
+    nl, cl = m.find_lines(10.0)
+    assert nl > 100
+    g = m.geometry()
+    cc = g["cc"]
+    lr = g["face_lr"]
+    nbrs = {}
+    for a, b in lr[m.nbface:]:
+        nbrs.setdefault(a, set()).add(b)
+        nbrs.setdefault(b, set()).add(a)
+    wall_cells = set(lr[:m.nbface, 0].tolist())
+    for k in range(nl):
+        cells = np.where(cl == k)[0]
+        assert len(cells) >= 2
+    # the cells of one line form a connected chain
+    k = int(cl[cl >= 0][0])
+    members = set(np.where(cl == k)[0].tolist())
+    assert any(x in wall_cells for x in members)
+    degree = [len(nbrs[x] & members) for x in members]
+    assert max(degree) <= 2 and degree.count(1) == 2
+    # no lines on an isotropic mesh
+    assert cases.channel(24, 8).find_lines(10.0)[0] == 0
+    # threshold <= 0 removes them
+    assert m.find_lines(0.0)[0] == 0
