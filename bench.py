@@ -301,12 +301,13 @@ def run_batched(fv, torch, dev, B=64, seed=7):
     z = np.load(os.path.join(ROOT, "tests", "golden", "naca0012_lam_hybrid_1_mesh.npz"))
     m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
                              z["btag"].astype(np.int32), reorder=1)
+    nlines = m.find_lines(10.0)[0]  # boundary-layer lines kept whole in the preconditioner's parts
     bcs = [(4, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))]
     rng = np.random.default_rng(seed)
     M, A, Re = rng.uniform(0.3, 0.7, B), rng.uniform(-4, 4, B), rng.uniform(2000, 10000, B)
     phs = [fv.physics_cfg(Minf=float(M[k]), aoa_deg=float(A[k]), Reinf=float(Re[k]), Tinf=288.15, Pr=0.72,
                           viscous=True) for k in range(B)]
-    res = {"mesh_cells": m.nelem, "batch": B}
+    res = {"mesh_cells": m.nelem, "batch": B, "lines": nlines}
     for tag, plist in (("single", phs[:1]), ("batch", phs)):
         start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), bcs)
         main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), bcs)

@@ -89,3 +89,37 @@ def test_fgmres_matches_oracle(cuda, kind):
     # classical Gram-Schmidt (PETSc default, no refinement): the recursive residual
     # estimate and the true residual part ways at tight tolerances
     assert np.linalg.norm(res) <= 1e-5 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("kind", ["ilu0", "sgs"])
+def test_line_aware_parts_match_oracle(cuda, kind):
+    """With lines of strongly coupled cells (findLines) on the reference's
+    laminar hybrid mesh, the parts take whole lines; the preconditioner is
+    still exactly the oracle's ILU(0) / SGS in the same elimination order."""
+    import torch
+    from tests import regression_cases as rc
+    m, c, regr = rc.load("laminar_naca0012_hybrid1")
+    nl, cl = m.find_lines(10.0)
+    assert nl > 100
+    ph = dict(Minf=0.5, Reinf=5000.0, viscous=True)
+    gd = fv.FlowFV(m, fv.physics_cfg(**ph), fv.numerics_cfg(flux="ROE"), c["bcs"])
+    od = orc.Disc(orc.Mesh.from_export(m.export()), **ph, flux="ROE", bcs=c["bcs"])
+    u = cases.perturbed_state(od.freestream(), m.nelem)
+    A = fv.BlockMatrix(gd, 8)
+    gd.assemble_jacobian(torch.tensor(u, device=cuda), A)
+    _, dt = od.residual(u)
+    A.add_diagonal(torch.tensor(m.geometry()["area"] / (100.0 * dt), device=cuda))
+    rp, col, val = A.to_host()
+    P = fv.Preconditioner(gd, A, kind, ordering=1, part_size=128)
+    P.setup()
+    order = P.order()
+    # every line's first piece (up to 128 cells) sits in consecutive positions of one part
+    pos = np.empty(m.nelem, np.int64)
+    pos[order] = np.arange(m.nelem)
+    first = np.where(cl == 0)[0]
+    assert pos[first].max() - pos[first].min() < 128
+    r = np.random.default_rng(5).normal(size=(m.nelem, 4))
+    z = torch.zeros((m.nelem, 4), dtype=torch.float64, device=cuda)
+    P.apply(torch.tensor(r, device=cuda), z)
+    zo = orc.precond_apply(rp, col, val, kind, r.ravel(), order=order).reshape(-1, 4)
+    assert np.abs(z.cpu().numpy() - zo).max() <= 1e-11 * np.abs(zo).max()
