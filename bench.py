@@ -296,7 +296,8 @@ def run_batched(fv, torch, dev, B=64, seed=7):
     """Batched solves of B laminar conditions (M ~ U[0.3, 0.7], AoA ~ U[-4, 4] deg,
     Re ~ U[2000, 10000], Pr 0.72, adiabatic wall; Roe, least squares) on the
     reference's hybrid NACA 0012 mesh (13,156 cells), all members in the same
-    launches, against one member alone."""
+    launches with FP32 Jacobians and ILU(0), against one member alone on the
+    FP32 path and on the plain FP64 path."""
     import collections
     z = np.load(os.path.join(ROOT, "tests", "golden", "naca0012_lam_hybrid_1_mesh.npz"))
     m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
@@ -308,19 +309,21 @@ def run_batched(fv, torch, dev, B=64, seed=7):
     phs = [fv.physics_cfg(Minf=float(M[k]), aoa_deg=float(A[k]), Reinf=float(Re[k]), Tinf=288.15, Pr=0.72,
                           viscous=True) for k in range(B)]
     res = {"mesh_cells": m.nelem, "batch": B, "lines": nlines}
-    for tag, plist in (("single", phs[:1]), ("batch", phs)):
+    for tag, plist, prec in (("single_plain_fp64", phs[:1], 8), ("single", phs[:1], 4), ("batch", phs, 4)):
         start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), bcs)
         main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), bcs)
         u = torch.tensor(np.concatenate([np.tile(x, (m.nelem, 1)) for x in main.freestream()]), device=dev)
         S1 = fv.SteadyBackwardEulerSolver(start, cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0,
-                                          max_timesteps=50, pc="ilu0", nl_update=2, precision=4)
-        S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=500, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
-                                          max_timesteps=600, pc="ilu0", nl_update=2, precision=4)
+                                          max_timesteps=50, pc="ilu0", nl_update=2, precision=prec)
+        S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
+                                          max_timesteps=600, pc="ilu0", nl_update=2, precision=prec)
         t, stats = _timed_solve(torch, [S1, S2], u, all_members=True)
         conv = sum(1 for st in stats if st["status"] == 0)
         res[tag] = {"seconds": t, "converged": conv, "members": len(plist), "converged_solves_s": conv / t,
                     "status_counts": dict(collections.Counter(int(st["status"]) for st in stats)),
                     "main_steps_max": max(st["steps"] for st in stats)}
+    res["batch_vs_single_plain_fp64"] = (res["batch"]["converged_solves_s"] /
+                                         max(res["single_plain_fp64"]["converged_solves_s"], 1e-30))
     return res
 
 
