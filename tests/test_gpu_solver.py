@@ -165,3 +165,23 @@ def test_cpp_interface_solves(cuda, tmp_path):
     out = subprocess.run([str(exe), "solve"], check=True, capture_output=True, text=True).stdout.split()
     steps, res = int(out[3]), float(out[4])
     assert 0 < steps < 1000 and res <= 1e-10
+
+
+def test_matrix_free_solve_matches_oracle(cuda):
+    """MatrixFreeSpatialJacobian::apply (alinalg.cpp:143-237) inside the steady
+    solve: the GPU's FP64 matrix-free solve and the oracle's take the same
+    number of steps (within two) and reach the same converged state."""
+    import torch
+    m, gd, od = _setup()
+    u0 = np.tile(od.freestream(), (m.nelem, 1))
+    S = fv.SteadyBackwardEulerSolver(gd, cfl_min=10, cfl_max=1000, tolerance=1e-10, max_timesteps=200,
+                                     pc="ilu0", precision=8, matrix_free=1)
+    ud = torch.tensor(u0, device=cuda)
+    rc, st = S.solve(ud)
+    P = fv.Preconditioner(gd, fv.BlockMatrix(gd, 8), "ilu0")
+    uo, sto = od.steady_solve(u0, cflmin=10, cflmax=1000, tol=1e-10, maxiter=200, pc="ilu0", matrix_free=True,
+                              order=P.order())
+    assert st[0]["status"] == 0 and sto["status"] == 0
+    assert abs(st[0]["steps"] - sto["steps"]) <= 2
+    ug = ud.cpu().numpy()
+    assert np.abs(ug - uo).max() / np.abs(uo).max() <= 1e-8
