@@ -182,7 +182,7 @@ def run_ours(args):
     e2e_value = reps.throughput(args.steps, t1 - t0)
     cl = main.surface_data(ud, 2)[0]
     u_conv = ud.clone()
-    variants = {} if args.no_variants else run_variants(fv, torch, dev, m, main, start, u0d, prec)
+    variants = {} if args.no_variants else run_variants(fv, torch, dev, m, main, start, u0d, prec, args)
     ud.copy_(u_conv)
 
     # per-kernel timing (roofline) at the converged state; time shares of one
@@ -275,7 +275,7 @@ def _timed_solve(torch, S_list, u, all_members=False):
     return ev0.elapsed_time(ev1) / 1e3, (sts[-1] if all_members else sts[-1][0])
 
 
-def run_variants(fv, torch, dev, m, main, start, u0d, prec):
+def run_variants(fv, torch, dev, m, main, start, u0d, prec, args):
     """(1) The same solve on the plain path: FP64 Jacobian and FP64 ILU(0),
     freestream start, one timed solve (CUDA events).  (2) Batched laminar
     solves (run_batched)."""
@@ -288,8 +288,51 @@ def run_variants(fv, torch, dev, m, main, start, u0d, prec):
     out["plain_fp64_cold"] = {"solves_s": 1.0 / t, "s_per_solve": t, "main_steps": st["steps"],
                               "linear_iters": st["lin_iters"], "converged": st["status"] == 0, "res": st["res"]}
     del P1, P2
-    out["batched_laminar"] = run_batched(fv, torch, dev)
+    out["batched_laminar"] = bl = run_batched(fv, torch, dev)
+    if args.warm_train > 0:
+        out["warm_start_laminar"] = run_warm_start(fv, torch, dev, args.warm_train, args.warm_test, args.warm_epochs,
+                                                   plain_single_s=bl["single_plain_fp64"]["seconds"])
     return out
+
+
+LAMINAR_BCS = [(4, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))]
+
+
+def _laminar_mesh(fv):
+    """The reference's hybrid NACA 0012 mesh (13,156 cells) with its
+    boundary-layer lines kept whole in the preconditioner's parts."""
+    z = np.load(os.path.join(ROOT, "tests", "golden", "naca0012_lam_hybrid_1_mesh.npz"))
+    m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
+                             z["btag"].astype(np.int32), reorder=1)
+    return m, m.find_lines(10.0)[0]
+
+
+def _laminar_conditions(fv, n, seed):
+    """n seeded laminar conditions: M ~ U[0.3, 0.7], AoA ~ U[-4, 4] deg,
+    Re ~ U[2000, 10000], Pr 0.72, T 288.15 K."""
+    rng = np.random.default_rng(seed)
+    M, A, Re = rng.uniform(0.3, 0.7, n), rng.uniform(-4, 4, n), rng.uniform(2000, 10000, n)
+    return [fv.physics_cfg(Minf=float(M[k]), aoa_deg=float(A[k]), Reinf=float(Re[k]), Tinf=288.15, Pr=0.72,
+                           viscous=True) for k in range(n)]
+
+
+def _laminar_solvers(fv, m, plist, prec, starter=True):
+    """(discretisation, [starter solver,] main solver) for the conditions plist:
+    first-order starter to a relative 1e-1 (at most 50 steps), then the
+    second-order main solve to the absolute 1e-10."""
+    main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), LAMINAR_BCS)
+    S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
+                                      max_timesteps=600, pc="ilu0", nl_update=2, precision=prec)
+    if not starter:
+        return main, [S2]
+    start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS)
+    S1 = fv.SteadyBackwardEulerSolver(start, cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0,
+                                      max_timesteps=50, pc="ilu0", nl_update=2, precision=prec)
+    return main, [S1, S2]
+
+
+def _freestream_field(torch, dev, disc, nelem):
+    return torch.tensor(np.concatenate([np.tile(x, (nelem, 1)) for x in disc.freestream()]), device=dev)
 
 
 def run_batched(fv, torch, dev, B=64, seed=7):
@@ -299,25 +342,13 @@ def run_batched(fv, torch, dev, B=64, seed=7):
     launches with FP32 Jacobians and ILU(0), against one member alone on the
     FP32 path and on the plain FP64 path."""
     import collections
-    z = np.load(os.path.join(ROOT, "tests", "golden", "naca0012_lam_hybrid_1_mesh.npz"))
-    m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
-                             z["btag"].astype(np.int32), reorder=1)
-    nlines = m.find_lines(10.0)[0]  # boundary-layer lines kept whole in the preconditioner's parts
-    bcs = [(4, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))]
-    rng = np.random.default_rng(seed)
-    M, A, Re = rng.uniform(0.3, 0.7, B), rng.uniform(-4, 4, B), rng.uniform(2000, 10000, B)
-    phs = [fv.physics_cfg(Minf=float(M[k]), aoa_deg=float(A[k]), Reinf=float(Re[k]), Tinf=288.15, Pr=0.72,
-                          viscous=True) for k in range(B)]
+    m, nlines = _laminar_mesh(fv)
+    phs = _laminar_conditions(fv, B, seed)
     res = {"mesh_cells": m.nelem, "batch": B, "lines": nlines}
     for tag, plist, prec in (("single_plain_fp64", phs[:1], 8), ("single", phs[:1], 4), ("batch", phs, 4)):
-        start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), bcs)
-        main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), bcs)
-        u = torch.tensor(np.concatenate([np.tile(x, (m.nelem, 1)) for x in main.freestream()]), device=dev)
-        S1 = fv.SteadyBackwardEulerSolver(start, cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0,
-                                          max_timesteps=50, pc="ilu0", nl_update=2, precision=prec)
-        S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
-                                          max_timesteps=600, pc="ilu0", nl_update=2, precision=prec)
-        t, stats = _timed_solve(torch, [S1, S2], u, all_members=True)
+        main, solvers = _laminar_solvers(fv, m, plist, prec)
+        u = _freestream_field(torch, dev, main, m.nelem)
+        t, stats = _timed_solve(torch, solvers, u, all_members=True)
         conv = sum(1 for st in stats if st["status"] == 0)
         res[tag] = {"seconds": t, "converged": conv, "members": len(plist), "converged_solves_s": conv / t,
                     "status_counts": dict(collections.Counter(int(st["status"]) for st in stats)),
@@ -325,6 +356,116 @@ def run_batched(fv, torch, dev, B=64, seed=7):
     res["batch_vs_single_plain_fp64"] = (res["batch"]["converged_solves_s"] /
                                          max(res["single_plain_fp64"]["converged_solves_s"], 1e-30))
     return res
+
+
+def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s=None):
+    """Learned warm start on the laminar hybrid NACA 0012 case.
+
+    n_train conditions (seed 11) are solved in batches of B from freestream
+    (starter + main); the converged members train the message-passing network
+    (4 layers, width 64; BF16 tensor-core GEMMs, FP32 accumulation, Adam) on
+    the GPU.  n_test held-out conditions (seed 12, same distributions) are then
+    solved twice in batches of B on the FP32-preconditioned path: from
+    freestream with the starter, and from the network's prediction without it.
+    Reported: nonlinear steps, wall time (CUDA events), initial-state error
+    relative to the converged state, the largest difference of the two
+    converged states and of their Cl/Cd, and the warm-started batch's rate
+    against one plain FP64 solve."""
+    import collections
+
+    from fvens_gb300.mpnn import MPNN, output_scale, train
+    m, _ = _laminar_mesh(fv)
+    phs_tr = _laminar_conditions(fv, n_train, 11)
+    phs_te = _laminar_conditions(fv, n_test, 12)
+    # training data: converged states of the batched solver
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    keep_phys, keep_u, gen_s = [], [], 0.0
+    for s in range(0, n_train, B):
+        plist = phs_tr[s:s + B]
+        main, solvers = _laminar_solvers(fv, m, plist, 4)
+        u = _freestream_field(torch, dev, main, m.nelem)
+        t, stats = _timed_solve(torch, solvers, u, all_members=True)
+        gen_s += t
+        uv = u.view(len(plist), m.nelem, 4)
+        for k, st in enumerate(stats):
+            if st["status"] == 0:
+                keep_phys.append(plist[k])
+                keep_u.append(uv[k].clone())
+        del main, solvers
+    targets = torch.stack(keep_u)
+    uinf = np.array([[1.0, np.cos(p.aoa), np.sin(p.aoa), 1.0 / (p.gamma * p.Minf ** 2) / (p.gamma - 1) + 0.5]
+                     for p in keep_phys])
+    net = MPNN(m, layers=4, wall_markers=(2,), seed=11)
+    net.set_scale(output_scale(targets.cpu().numpy(), uinf))
+    a, b = ev(), ev()
+    a.record()
+    losses = train(net, keep_phys, targets, epochs=epochs, batch=16, lr=2e-3, lr_final=1e-4, seed=0)
+    b.record()
+    torch.cuda.synchronize()
+    train_s = a.elapsed_time(b) / 1e3
+    # held-out conditions: freestream + starter vs prediction, batches of B
+    out = {"train_conditions": n_train, "train_converged": len(keep_phys), "test_conditions": n_test,
+           "epochs": epochs, "train_batch": 16, "params": net.nparams, "data_generation_s": gen_s,
+           "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
+    agg = {k: dict(seconds=0.0, steps=[], status=collections.Counter()) for k in ("freestream", "warm")}
+    err_ratio, du_max, dcl_max, pred_s = [], 0.0, 0.0, 0.0
+    for s in range(0, n_test, B):
+        plist = phs_te[s:s + B]
+        nb = len(plist)
+        main, solvers = _laminar_solvers(fv, m, plist, 4)
+        u_free = _freestream_field(torch, dev, main, m.nelem)
+        u0_free = u_free.clone()
+        t, st_free = _timed_solve(torch, solvers, u_free, all_members=True)
+        agg["freestream"]["seconds"] += t
+        main_w, solvers_w = _laminar_solvers(fv, m, plist, 4, starter=False)
+        u_warm = torch.empty_like(u_free)
+        a, b = ev(), ev()
+        a.record()
+        net.predict(plist, u_warm)
+        b.record()
+        torch.cuda.synchronize()
+        pred_s += a.elapsed_time(b) / 1e3
+        u0_warm = u_warm.clone()
+        t, st_warm = _timed_solve(torch, solvers_w, u_warm, all_members=True)
+        agg["warm"]["seconds"] += t + a.elapsed_time(b) / 1e3
+        # freestream stats from the main solver (the starter's steps added)
+        for tag, sts in (("freestream", st_free), ("warm", st_warm)):
+            agg[tag]["status"].update(int(x["status"]) for x in sts)
+            agg[tag]["steps"] += [int(x["steps"]) for x in sts]
+        uf = u_free.view(nb, m.nelem, 4)
+        uw = u_warm.view(nb, m.nelem, 4)
+        for k in range(nb):
+            if st_free[k]["status"] != 0:
+                continue
+            ref = uf[k]
+            e0 = torch.linalg.norm(u0_free.view(nb, m.nelem, 4)[k] - ref)
+            e1 = torch.linalg.norm(u0_warm.view(nb, m.nelem, 4)[k] - ref)
+            err_ratio.append(float(e1 / e0))
+            if st_warm[k]["status"] == 0:
+                du_max = max(du_max, float((uw[k] - ref).abs().max() / ref.abs().max()))
+        cf = main.surface_data(u_free, 2)
+        cw = main_w.surface_data(u_warm, 2)
+        for k in range(nb):
+            if st_free[k]["status"] == 0 and st_warm[k]["status"] == 0:
+                dcl_max = max(dcl_max, float(np.max(np.abs(cw[k, :2] - cf[k, :2]) / np.maximum(np.abs(cf[k, :2]),
+                                                                                                 1e-12))))
+        del main, solvers, main_w, solvers_w
+    for tag in agg:
+        conv = agg[tag]["status"].get(0, 0)
+        st = agg[tag]
+        out[tag] = {"seconds": st["seconds"], "converged": conv, "converged_solves_s": conv / st["seconds"],
+                    "main_steps_mean": float(np.mean(st["steps"])), "main_steps_max": int(np.max(st["steps"])),
+                    "status_counts": {str(k): v for k, v in st["status"].items()}}
+    out["freestream"]["note"] = "main-solve steps; a first-order starter ran before each batch"
+    out["warm"]["prediction_s"] = pred_s
+    out["initial_error_ratio_mean"] = float(np.mean(err_ratio)) if err_ratio else None
+    out["initial_error_ratio_max"] = float(np.max(err_ratio)) if err_ratio else None
+    out["converged_state_max_rel_diff"] = du_max
+    out["cl_cdp_max_rel_diff"] = dcl_max
+    out["warm_vs_freestream"] = out["warm"]["converged_solves_s"] / max(out["freestream"]["converged_solves_s"], 1e-30)
+    if plain_single_s:
+        out["warm_batch_vs_single_plain_fp64"] = out["warm"]["converged_solves_s"] * plain_single_s
+    return out
 
 
 def _oracle_case(m):
@@ -433,6 +574,10 @@ def main():
                     help="main-solve Krylov iterations per solve assumed by the reference arm")
     ap.add_argument("--ref-starter-iters", type=int, default=1800,
                     help="starter Krylov iterations per solve assumed by the reference arm")
+    ap.add_argument("--warm-train", type=int, default=512,
+                    help="training conditions of the learned warm-start variant (0 skips it; 2048 for the full set)")
+    ap.add_argument("--warm-test", type=int, default=64, help="held-out conditions of the warm-start variant")
+    ap.add_argument("--warm-epochs", type=int, default=60, help="training epochs of the warm-start network")
     args = ap.parse_args()
     if args.max_main_steps > 0:
         MAIN["max_timesteps"] = args.max_main_steps

@@ -319,6 +319,37 @@ fv_status fv_pointwise_flux_jacobian(fv_disc *d, int kind, int n, const double *
 fv_status fv_pointwise_bc(fv_disc *d, int bc_type, const double *bc_vals, int n, const double *d_in,
                           const double *d_nrm, double *d_ghost, double *d_jac_ghost, double *d_dgdu);
 
+/* ---- learned warm start (no counterpart in the reference) ----
+ * A message-passing network on the mesh's cell graph predicts the converged
+ * state of flow conditions (Minf, aoa, Reinf of fv_physics_cfg); the steady
+ * solver starts from the prediction instead of freestream.  Width 64, `layers`
+ * message-passing layers, BF16 tensor-core GEMMs with FP32 accumulation,
+ * trained with Adam on states the solver converged.  The output y is the
+ * state's deviation from freestream over a per-variable scale:
+ * u = uinf + scale * y. */
+typedef struct fv_mpnn fv_mpnn;
+/* wall_markers: boundary markers whose faces give the wall-distance feature */
+fv_status fv_mpnn_create(fv_mesh *m, int layers, const int *wall_markers, int nwall, unsigned long long seed,
+                         fv_mpnn **out);
+void fv_mpnn_destroy(fv_mpnn *n);
+fv_status fv_mpnn_set_scale(fv_mpnn *n, const float *h_scale4);
+/* copies the flat FP32 parameter vector in (h_in != NULL) and then out
+ * (h_out != NULL); *count receives its length */
+fv_status fv_mpnn_params(fv_mpnn *n, float *h_out, const float *h_in, long long *count);
+/* graph inputs: cell features nelem x 4, interior faces (L, R) nf x 2, face
+ * features nf x 3 (any may be NULL) */
+fv_status fv_mpnn_graph(const fv_mpnn *n, float *h_xs, int *h_faces, float *h_eattr);
+/* d_u: batch x nelem x 4 predicted conserved states.  Synchronises. */
+fv_status fv_mpnn_predict(fv_mpnn *n, const fv_physics_cfg *phys, int batch, double *d_u);
+/* gradient (h_grad, length of fv_mpnn_params) and value (h_loss) of the mean
+ * squared error of y against the targets d_target (batch x nelem x 4 conserved
+ * states); either output may be NULL.  Synchronises. */
+fv_status fv_mpnn_gradients(fv_mpnn *n, const fv_physics_cfg *phys, int batch, const double *d_target,
+                            float *h_grad, float *h_loss);
+/* one Adam step (beta 0.9, 0.999, eps 1e-8) with learning rate lr */
+fv_status fv_mpnn_train_step(fv_mpnn *n, const fv_physics_cfg *phys, int batch, const double *d_target, float lr,
+                             float *h_loss);
+
 #ifdef __cplusplus
 }
 #endif
