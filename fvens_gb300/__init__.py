@@ -283,6 +283,46 @@ class FlowFV:
         check(lib().fv_surface_data(self._h, _vp(dptr(u)), int(wall_marker), _hp(out, ctypes.c_double)))
         return out
 
+    def surface_distribution(self, u, wall_marker, member=0):
+        """Rows (x, y, Cp, Cf) of the faces of wall_marker (the per-face output
+        of computeSurfaceData), for one batch member."""
+        n = ctypes.c_int()
+        check(lib().fv_surface_distribution(self._h, None, int(wall_marker), int(member), None, ctypes.byref(n)))
+        out = np.zeros((n.value, 4))
+        check(lib().fv_surface_distribution(self._h, _vp(dptr(u)), int(wall_marker), int(member),
+                                            _hp(out, ctypes.c_double), ctypes.byref(n)))
+        return out
+
+    def export_surface_data(self, u, wall_markers, other_markers, basename, member=0):
+        """FlowOutput::exportSurfaceData (aoutput.cpp:181-298): for each wall
+        marker the file <basename>-surf_w<marker>.out with rows x, y, Cp, Cf and
+        the Cl, Cdp, Cdf trailer; for each other marker <basename>-surf_o<marker>.out
+        with the face centres and the velocity of the faces' cells.  Returns
+        {marker: (Cl, Cdp, Cdf)} of the wall markers."""
+        g = lambda v: format(float(v), ".6g")
+        out = {}
+        for wm in wall_markers:
+            rows = self.surface_distribution(u, wm, member)
+            cl = self.surface_data(u, wm)[member]
+            with open(f"{basename}-surf_w{wm}.out", "w") as f:
+                f.write("#  x \t y \t Cp  \t Cf \n")
+                for r in rows:
+                    f.write("".join("  " + g(v) for v in r) + "\n")
+                f.write("# Cl      Cdp      Cdf\n")
+                f.write(f"# {g(cl[0])}  {g(cl[1])}  {g(cl[2])}\n")
+            out[wm] = tuple(float(x) for x in cl)
+        if other_markers:
+            ex, geo = self.mesh.export(), self.mesh.geometry()
+            uh = u.detach().cpu().numpy().reshape(self.batch, self.nelem, 4)[member]
+            fc = ex["coords"][ex["bface"]].mean(axis=1)
+            for om in other_markers:
+                with open(f"{basename}-surf_o{om}.out", "w") as f:
+                    f.write("#   x         y          u           v\n")
+                    for k in np.nonzero(ex["btag"] == om)[0]:
+                        c = uh[geo["face_lr"][k, 0]]
+                        f.write("".join("  " + g(v) for v in (fc[k, 0], fc[k, 1], c[1] / c[0], c[2] / c[0])) + "\n")
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None) is not None and _lib is not None:
             _lib.fv_disc_destroy(self._h)

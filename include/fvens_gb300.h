@@ -190,6 +190,13 @@ fv_status fv_get_gradients(fv_disc *d, const double *d_u, double *d_grad, int pr
  * wall_marker, from the cell-centred state and its conserved gradients, FP64.
  * h_out[3*batch] = (Cl, CDp, CDsf) per condition (host).  Synchronises. */
 fv_status fv_surface_data(fv_disc *d, const double *d_u, int wall_marker, double *h_out);
+/* The per-face output of computeSurfaceData (flow_spatial.cpp:168-237), the
+ * rows of FlowOutput::exportSurfaceData's wall files (aoutput.cpp:181-238):
+ * h_out[4*nfaces] = (x, y, Cp, Cf) of each boundary face of wall_marker in
+ * boundary-face order, for batch member `member`.  *nfaces receives the face
+ * count; h_out == NULL only counts.  Synchronises. */
+fv_status fv_surface_distribution(fv_disc *d, const double *d_u, int wall_marker, int member, double *h_out,
+                                  int *nfaces);
 /* FlowOutput::compute_entropy_cell (aoutput.cpp:28-62): sqrt(sum_i
  * ((s_i - s_inf)/s_inf)^2 A_i), s = p / rho^gamma, per condition into
  * h_err[batch] (host).  Uses the residual scratch.  Synchronises. */

@@ -212,8 +212,17 @@ class Disc:
 
     def surface_data(self, u, marker):
         out = np.zeros(3)
-        lib().orc_surface_data(self._h, p(np.ascontiguousarray(u, np.float64)), int(marker), p(out))
+        lib().orc_surface_data(self._h, p(np.ascontiguousarray(u, np.float64)), int(marker), p(out), None)
         return out
+
+    def surface_distribution(self, u, marker):
+        """Per-face rows (x, y, Cp, Cf) of the marker's faces."""
+        u = np.ascontiguousarray(u, np.float64)
+        out = np.zeros(3)
+        n = lib().orc_surface_data(self._h, p(u), int(marker), p(out), None)
+        rows = np.zeros((n, 4))
+        lib().orc_surface_data(self._h, p(u), int(marker), p(out), p(rows))
+        return rows
 
     def entropy_error(self, u):
         return lib().orc_entropy_error(self._h, p(np.ascontiguousarray(u, np.float64)))

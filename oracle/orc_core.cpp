@@ -1500,8 +1500,10 @@ int orc_tvdrk(const void *h, int order, double cfl, double final_time, double *u
 	return status;
 }
 
-/* FlowFV_base::computeSurfaceData, flow_spatial.cpp:130-310: returns Cl, CDp, CDsf */
-int orc_surface_data(const void *h, const double *u, int marker, double *out3)
+/* FlowFV_base::computeSurfaceData, flow_spatial.cpp:130-310: returns Cl, CDp, CDsf,
+ * and (rows != NULL) the per-face output x, y, Cp, Cf of the marker's faces
+ * (flow_spatial.cpp:168-237); returns the face count */
+int orc_surface_data(const void *h, const double *u, int marker, double *out3, double *rows)
 {
 	const Disc *d = (const Disc *)h;
 	const Mesh &M = *d->m;
@@ -1511,6 +1513,7 @@ int orc_surface_data(const void *h, const double *u, int marker, double *out3)
 	const double pinf = 1.0 / (d->P.g * d->P.Minf * d->P.Minf);
 	const double fnorm[2] = {-wind[1], wind[0]};
 	double Cl = 0, Cdp = 0, Cdf = 0, tot = 0;
+	int nrow = 0;
 	for (int f = 0; f < M.nbface; f++) {
 		if (M.btag[f] != marker) continue;
 		const int le = M.intfac[4 * f];
@@ -1534,13 +1537,22 @@ int orc_surface_data(const void *h, const double *u, int marker, double *out3)
 		const double ndotw = n[0] * wind[0] + n[1] * wind[1];
 		const double ndotnw = n[0] * fnorm[0] + n[1] * fnorm[1];
 		const double tdotw = tg[0] * wind[0] + tg[1] * wind[1];
+		if (rows) {
+			const int p0 = M.intfac[4 * f + 2], p1 = M.intfac[4 * f + 3];
+			double *r = rows + 4 * (size_t)nrow;
+			r[0] = (M.coords[2 * p0] + M.coords[2 * p1]) / 2;
+			r[1] = (M.coords[2 * p0 + 1] + M.coords[2 * p1 + 1]) / 2;
+			r[2] = cp;
+			r[3] = cf;
+		}
+		nrow++;
 		tot += ar;
 		Cl += cp * ndotnw * ar;
 		Cdp += cp * ndotw * ar;
 		Cdf += cf * tdotw * ar;
 	}
 	out3[0] = Cl / tot; out3[1] = Cdp / tot; out3[2] = Cdf / tot;
-	return 0;
+	return nrow;
 }
 
 /* FlowOutput::compute_entropy_cell, aoutput.cpp:28-62 */
