@@ -407,7 +407,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
     out = {"train_conditions": n_train, "train_converged": len(keep_phys), "test_conditions": n_test,
            "epochs": epochs, "train_batch": 16, "params": net.nparams, "data_generation_s": gen_s,
            "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
-    agg = {k: dict(seconds=0.0, steps=[], status=collections.Counter()) for k in ("freestream", "warm")}
+    agg = {k: dict(seconds=0.0, steps=[], res0=[], status=collections.Counter()) for k in ("freestream", "warm")}
     err_ratio, du_max, dcl_max, pred_s = [], 0.0, 0.0, 0.0
     for s in range(0, n_test, B):
         plist = phs_te[s:s + B]
@@ -432,6 +432,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
         for tag, sts in (("freestream", st_free), ("warm", st_warm)):
             agg[tag]["status"].update(int(x["status"]) for x in sts)
             agg[tag]["steps"] += [int(x["steps"]) for x in sts]
+            agg[tag]["res0"] += [float(x["res0"]) for x in sts if x["res0"] > 0]
         uf = u_free.view(nb, m.nelem, 4)
         uw = u_warm.view(nb, m.nelem, 4)
         for k in range(nb):
@@ -455,6 +456,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
         st = agg[tag]
         out[tag] = {"seconds": st["seconds"], "converged": conv, "converged_solves_s": conv / st["seconds"],
                     "main_steps_mean": float(np.mean(st["steps"])), "main_steps_max": int(np.max(st["steps"])),
+                    "main_initial_residual_geomean": float(np.exp(np.mean(np.log(st["res0"])))) if st["res0"] else None,
                     "status_counts": {str(k): v for k, v in st["status"].items()}}
     out["freestream"]["note"] = "main-solve steps; a first-order starter ran before each batch"
     out["warm"]["prediction_s"] = pred_s

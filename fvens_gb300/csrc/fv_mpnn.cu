@@ -44,6 +44,8 @@ constexpr int KUPD = 128;    // update inputs
 constexpr int NDEC = 8;      // decoder outputs 4, padded
 constexpr int GT = 128;      // GEMM CTA threads (4 warps x 16 rows)
 constexpr int GR = 64;       // GEMM rows per CTA
+constexpr int kWgradCtas = 608;  // weight-gradient CTAs (4 per SM of 152), each over many row chunks
+constexpr int kReduceSlices = 16;  // slices of the CTA partials in the gradient reduction
 
 __device__ __forceinline__ unsigned pack_bf16(float lo, float hi)
 {
@@ -145,128 +147,321 @@ __device__ __forceinline__ void msg_ends(const Graph &G, int m, int &src, int &d
 	else { src = lr.x; dst = lr.y; }
 }
 
-// ------------------------------- forward kernels -------------------------------
+// --------------------------------- row operands ---------------------------------
+/* Row operands of the GEMMs come from loaders: quad(r, ri, q) returns the
+ * columns 4q..4q+3 of row r (FP32); prep(r, ri) fills per-row data that a
+ * tile's loads share (message ends), once per row and tile. */
+struct RowInfo {
+	int src, dst;   // message source / destination rows (member offset included)
+	float4 e;       // message edge features
+};
 
-/* h0 = relu(We x + be); x = static features + condition features */
-__global__ void __launch_bounds__(GT) k_encode(Graph G, int B, const float *cond /*[B][3]*/, const float *We,
-                                               const float *be, float *h, float *pre)
-{
-	__shared__ __align__(16) __nv_bfloat16 sA[GR * (KENC + 8)], sB[W * (KENC + 8)];
-	const int rows = B * G.nc, row0 = blockIdx.x * GR;
-	for (int e = threadIdx.x; e < GR * KENC; e += GT) {
-		const int rr = e / KENC, k = e - rr * KENC, r = row0 + rr;
-		float v = 0.f;
-		if (r < rows && k < 7) {
-			const int b = r / G.nc, i = r - b * G.nc;
-			const float4 s = G.xs[i];
-			v = k == 0 ? s.x : k == 1 ? s.y : k == 2 ? s.z : k == 3 ? s.w : cond[3 * b + (k - 4)];
-		}
-		sA[rr * (KENC + 8) + k] = __float2bfloat16_rn(v);
+struct LEnc {  // [xs (4), M, AoA, Re (3), 0...]: K = 16
+	Graph G;
+	const float *cond;
+	__device__ void prep(int, RowInfo &) const {}
+	__device__ float4 quad(int r, const RowInfo &, int q) const
+	{
+		const int b = r / G.nc, i = r - b * G.nc;
+		if (q == 0) return G.xs[i];
+		if (q == 1) return make_float4(cond[3 * b], cond[3 * b + 1], cond[3 * b + 2], 0.f);
+		return make_float4(0.f, 0.f, 0.f, 0.f);
 	}
-	stage_w<KENC, W>(We, 7, W, 7, sB);
+};
+struct LMsg {  // [h_src (64), h_dst (64), e (3), 0...]: K = 144
+	Graph G;
+	const float *h;
+	__device__ void prep(int r, RowInfo &ri) const
+	{
+		const int per = 2 * G.nf, b = r / per;
+		msg_ends(G, r - b * per, ri.src, ri.dst, ri.e);
+		ri.src += b * G.nc;
+		ri.dst += b * G.nc;
+	}
+	__device__ float4 quad(int, const RowInfo &ri, int q) const
+	{
+		if (q < W / 4) return reinterpret_cast<const float4 *>(h + (size_t)ri.src * W)[q];
+		if (q < W / 2) return reinterpret_cast<const float4 *>(h + (size_t)ri.dst * W)[q - W / 4];
+		if (q == W / 2) return make_float4(ri.e.x, ri.e.y, ri.e.z, 0.f);
+		return make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+};
+struct LUpd {  // [h (64), a (64)]: K = 128
+	const float *h, *agg;
+	__device__ void prep(int, RowInfo &) const {}
+	__device__ float4 quad(int r, const RowInfo &, int q) const
+	{
+		return q < W / 4 ? reinterpret_cast<const float4 *>(h + (size_t)r * W)[q]
+		                 : reinterpret_cast<const float4 *>(agg + (size_t)r * W)[q - W / 4];
+	}
+};
+struct LRows {  // plain rows x[r][0..nz) (row stride ld, both multiples of 4), zero beyond
+	const float *x;
+	int ld, nz;
+	__device__ void prep(int, RowInfo &) const {}
+	__device__ float4 quad(int r, const RowInfo &, int q) const
+	{
+		return 4 * q < nz ? reinterpret_cast<const float4 *>(x + (size_t)r * ld)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+};
+struct LRelu {  // dZ = dY (Z > 0), rows of width 64
+	const float *dy, *z;
+	__device__ void prep(int, RowInfo &) const {}
+	__device__ float4 quad(int r, const RowInfo &, int q) const
+	{
+		const float4 d = reinterpret_cast<const float4 *>(dy + (size_t)r * W)[q];
+		const float4 zz = reinterpret_cast<const float4 *>(z + (size_t)r * W)[q];
+		return make_float4(zz.x > 0.f ? d.x : 0.f, zz.y > 0.f ? d.y : 0.f, zz.z > 0.f ? d.z : 0.f,
+		                   zz.w > 0.f ? d.w : 0.f);
+	}
+};
+struct LMsgGrad {  // dZm = d(aggregate) of the destination, masked by Zm > 0
+	Graph G;
+	const float *dagg;  // [B*nc][lda], the aggregate's columns from off
+	int lda, off;
+	const float *z;     // Zm [B*2nf][64]
+	__device__ void prep(int r, RowInfo &ri) const
+	{
+		const int per = 2 * G.nf, b = r / per;
+		msg_ends(G, r - b * per, ri.src, ri.dst, ri.e);
+		ri.dst += b * G.nc;
+	}
+	__device__ float4 quad(int r, const RowInfo &ri, int q) const
+	{
+		const float4 d = reinterpret_cast<const float4 *>(dagg + (size_t)ri.dst * lda + off)[q];
+		const float4 zz = reinterpret_cast<const float4 *>(z + (size_t)r * W)[q];
+		return make_float4(zz.x > 0.f ? d.x : 0.f, zz.y > 0.f ? d.y : 0.f, zz.z > 0.f ? d.z : 0.f,
+		                   zz.w > 0.f ? d.w : 0.f);
+	}
+};
+
+/* stages the rows of a 64-row tile as bf16 [64][K + 8] (8-byte stores) */
+template <int K, class L>
+__device__ __forceinline__ void stage_rows(const L &ld, int row0, int rows, RowInfo *ri, __nv_bfloat16 *sA)
+{
+	if (threadIdx.x < GR && row0 + (int)threadIdx.x < rows) ld.prep(row0 + threadIdx.x, ri[threadIdx.x]);
 	__syncthreads();
-	float c[W / 8][4];
-	tile_mma<KENC, W>(sA, sB, c);
-	tile_store<W>(c, row0, rows, be, h, W, W, pre, 1);
+	for (int e = threadIdx.x; e < GR * (K / 4); e += GT) {
+		const int rr = e / (K / 4), q = e - rr * (K / 4), r = row0 + rr;
+		const float4 v = r < rows ? ld.quad(r, ri[rr], q) : make_float4(0.f, 0.f, 0.f, 0.f);
+		*reinterpret_cast<uint2 *>(sA + rr * (K + 8) + 4 * q) = make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
+	}
 }
 
-/* messages: Zm = Wm [h_src, h_dst, e] + bm, m = relu(Zm); rows = B * 2 nf */
-__global__ void __launch_bounds__(GT) k_message(Graph G, int B, const float *h, const float *Wm, const float *bm,
-                                                float *msg, float *pre)
+// ----------------------------------- epilogues -----------------------------------
+struct EStore {  // out = act(Z + bias) (pre = Z + bias when given), columns < ncols (even)
+	const float *bias;
+	float *out, *pre;
+	int ldo, ncols, relu;
+	__device__ void operator()(int r, int n, float z0, float z1) const  // columns n, n + 1 (n even)
+	{
+		if (n >= ncols) return;
+		const float2 v = make_float2(z0 + (bias ? bias[n] : 0.f), z1 + (bias ? bias[n + 1] : 0.f));
+		if (pre) *reinterpret_cast<float2 *>(pre + (size_t)r * ldo + n) = v;
+		*reinterpret_cast<float2 *>(out + (size_t)r * ldo + n) =
+		    relu ? make_float2(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f)) : v;
+	}
+};
+struct EUpdate {  // hn = h + relu(Z + bu), pre = Z + bu
+	const float *bias, *h;
+	float *hn, *pre;
+	__device__ void operator()(int r, int n, float z0, float z1) const
+	{
+		const float2 v = make_float2(z0 + bias[n], z1 + bias[n + 1]);
+		const float2 hh = *reinterpret_cast<const float2 *>(h + (size_t)r * W + n);
+		*reinterpret_cast<float2 *>(pre + (size_t)r * W + n) = v;
+		*reinterpret_cast<float2 *>(hn + (size_t)r * W + n) = make_float2(hh.x + fmaxf(v.x, 0.f), hh.y + fmaxf(v.y, 0.f));
+	}
+};
+
+// ------------------------------------ kernels ------------------------------------
+/* Z = A W^T over persistent 64-row tiles: the CTA stages its weight operand once
+ * (W [N][K], or with TRANS the transpose of W [K][N]: the input-gradient GEMM
+ * dX = dZ W), then loops over tiles blockIdx.x, blockIdx.x + gridDim.x, ... */
+template <int K, int N, bool TRANS, class L, class E>
+__global__ void __launch_bounds__(GT) k_gemm(int rows, L ld, const float *w, int ldw, int nvalid, int kvalid, E ep)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
-	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);
-	__nv_bfloat16 *sB = sA + GR * (KMSG + 8);
-	const int per = 2 * G.nf, rows = B * per, row0 = blockIdx.x * GR;
-	for (int e = threadIdx.x; e < GR * KMSG; e += GT) {
-		const int rr = e / KMSG, k = e - rr * KMSG, r = row0 + rr;
-		float v = 0.f;
-		if (r < rows) {
-			const int b = r / per, mid = r - b * per;
-			int s, d;
-			float4 ev;
-			msg_ends(G, mid, s, d, ev);
-			const float *hb = h + (size_t)b * G.nc * W;
-			if (k < W) v = hb[(size_t)s * W + k];
-			else if (k < 2 * W) v = hb[(size_t)d * W + (k - W)];
-			else if (k == 2 * W) v = ev.x;
-			else if (k == 2 * W + 1) v = ev.y;
-			else if (k == 2 * W + 2) v = ev.z;
+	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);  // [64][K + 8]
+	__nv_bfloat16 *sB = sA + GR * (K + 8);                         // [N][K + 8]
+	__shared__ RowInfo ri[GR];
+	if (!TRANS) {
+		stage_w<K, N>(w, ldw, nvalid, kvalid, sB);
+	} else {
+		for (int e = threadIdx.x; e < N * K; e += GT) {
+			const int k = e / N, n = e - k * N;  // consecutive threads: consecutive columns of W's row k
+			sB[n * (K + 8) + k] = __float2bfloat16_rn((n < nvalid && k < kvalid) ? w[(size_t)k * ldw + n] : 0.f);
 		}
-		sA[rr * (KMSG + 8) + k] = __float2bfloat16_rn(v);
 	}
-	stage_w<KMSG, W>(Wm, 2 * W + 3, W, 2 * W + 3, sB);
-	__syncthreads();
-	float c[W / 8][4];
-	tile_mma<KMSG, W>(sA, sB, c);
-	tile_store<W>(c, row0, rows, bm, msg, W, W, pre, 1);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	for (int row0 = blockIdx.x * GR; row0 < rows; row0 += gridDim.x * GR) {
+		__syncthreads();  // the previous tile's operands are consumed
+		stage_rows<K>(ld, row0, rows, ri, sA);
+		__syncthreads();
+		float c[N / 8][4];
+		tile_mma<K, N>(sA, sB, c);
+		for (int nt = 0; nt < N / 8; nt++)
+			for (int hh = 0; hh < 2; hh++) {
+				const int r = row0 + warp * 16 + g + 8 * hh;
+				if (r >= rows) continue;
+				ep(r, nt * 8 + 2 * t, c[nt][2 * hh], c[nt][2 * hh + 1]);
+			}
+	}
 }
 
-/* a_i = sum of the messages into cell i (fixed CSR order) */
-__global__ void k_aggregate(Graph G, int B, const float *msg, float *agg)
+__device__ __forceinline__ void ldsm_x4_trans(unsigned *r, const __nv_bfloat16 *p)
 {
-	const int r = blockIdx.x, k = threadIdx.x;  // one block of 64 threads per (member, cell)
-	const int b = r / G.nc, i = r - b * G.nc;
-	const float *mb = msg + (size_t)b * 2 * G.nf * W;
+	const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+	asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+	             : "r"(a));
+}
+
+/* Weight gradients dW[n][k] = sum_r dZ[r][n] X[r][k] and db[n] = sum_r dZ[r][n]:
+ * the CTA accumulates its 64-row chunks blockIdx.x, blockIdx.x + gridDim.x, ...
+ * in registers and writes one partial [N][K] (+ [N] for the bias).  Both
+ * operands are staged row-major ([64][N + 8], [64][K + 8]); the MMA fragments
+ * of their transposes come from ldmatrix.trans.  The chunk-to-CTA assignment
+ * depends only on the row count and the grid, so the sums are reproducible;
+ * the bias sums dZ in FP32. */
+template <int K, int N, class XL, class ZL>
+__global__ void __launch_bounds__(GT) k_wgrad(int rows, XL xl, ZL zl, float *part, float *bpart)
+{
+	static_assert(GT % (N / 4) == 0, "a thread stages the same column quad of dZ in every row");
+	extern __shared__ __align__(16) unsigned char smem[];
+	__nv_bfloat16 *sZ = reinterpret_cast<__nv_bfloat16 *>(smem);  // [64][N + 8]
+	__nv_bfloat16 *sX = sZ + GR * (N + 8);                         // [64][K + 8]
+	__shared__ RowInfo ri[GR];
+	__shared__ float4 sbias[GT];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int nchunks = (rows + GR - 1) / GR;
+	// warp w owns the output rows n in [16 w, 16 w + 16) (N = 64: 4 warps; N = 16: warp 0)
+	float c[K / 8][4];
+	for (int nt = 0; nt < K / 8; nt++)
+		for (int q = 0; q < 4; q++) c[nt][q] = 0.f;
+	float4 bsum = make_float4(0.f, 0.f, 0.f, 0.f);
+	// ldmatrix row addresses: lane i -> matrix i / 8, row i % 8
+	const int mi = lane >> 3, mr = lane & 7;
+	for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+		const int row0 = ch * GR;
+		__syncthreads();
+		if (threadIdx.x < GR && row0 + (int)threadIdx.x < rows) {
+			xl.prep(row0 + threadIdx.x, ri[threadIdx.x]);
+		}
+		__syncthreads();
+		for (int e = threadIdx.x; e < GR * (K / 4); e += GT) {
+			const int rr = e / (K / 4), q = e - rr * (K / 4), r = row0 + rr;
+			const float4 v = r < rows ? xl.quad(r, ri[rr], q) : make_float4(0.f, 0.f, 0.f, 0.f);
+			*reinterpret_cast<uint2 *>(sX + rr * (K + 8) + 4 * q) = make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
+		}
+		__syncthreads();  // zl.prep may overwrite ri (message ends of the same rows)
+		if (threadIdx.x < GR && row0 + (int)threadIdx.x < rows) zl.prep(row0 + threadIdx.x, ri[threadIdx.x]);
+		__syncthreads();
+		for (int e = threadIdx.x; e < GR * (N / 4); e += GT) {
+			const int rr = e / (N / 4), q = e - rr * (N / 4), r = row0 + rr;
+			const float4 v = r < rows ? zl.quad(r, ri[rr], q) : make_float4(0.f, 0.f, 0.f, 0.f);
+			bsum.x += v.x; bsum.y += v.y; bsum.z += v.z; bsum.w += v.w;
+			*reinterpret_cast<uint2 *>(sZ + rr * (N + 8) + 4 * q) = make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
+		}
+		__syncthreads();
+		if (warp * 16 < N) {
+			for (int k0 = 0; k0 < GR; k0 += 16) {
+				// A = dZ^T (16 x 16 at rows n0.., k = data rows k0..): matrices (k0, n0), (k0, n0+8), (k0+8, n0), (k0+8, n0+8)
+				unsigned af[4];
+				ldsm_x4_trans(af, sZ + (k0 + mr + ((mi & 2) ? 8 : 0)) * (N + 8) + warp * 16 + ((mi & 1) ? 8 : 0));
+				for (int nt = 0; nt < K / 8; nt += 2) {
+					// B = X (k = data rows): matrices (k0, f0), (k0+8, f0), (k0, f0+8), (k0+8, f0+8)
+					unsigned bf[4];
+					ldsm_x4_trans(bf, sX + (k0 + mr + ((mi & 1) ? 8 : 0)) * (K + 8) + nt * 8 + ((mi & 2) ? 8 : 0));
+					mma_bf16(c[nt], af, bf);
+					mma_bf16(c[nt + 1], af, bf + 2);
+				}
+			}
+		}
+	}
+	const int g = lane >> 2, t = lane & 3;
+	if (warp * 16 < N) {
+		float *pc = part + (size_t)blockIdx.x * N * K;
+		for (int nt = 0; nt < K / 8; nt++)
+			for (int hh = 0; hh < 2; hh++)
+				for (int j = 0; j < 2; j++) pc[(size_t)(warp * 16 + g + 8 * hh) * K + nt * 8 + 2 * t + j] = c[nt][2 * hh + j];
+	}
+	// bias: threads with the same column quad (threadIdx.x mod N/4) hold partials of different rows
+	sbias[threadIdx.x] = bsum;
+	__syncthreads();
+	if (threadIdx.x < N / 4) {
+		float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+		for (int j = threadIdx.x; j < GT; j += N / 4) {
+			s.x += sbias[j].x; s.y += sbias[j].y; s.z += sbias[j].z; s.w += sbias[j].w;
+		}
+		reinterpret_cast<float4 *>(bpart + (size_t)blockIdx.x * N)[threadIdx.x] = s;
+	}
+}
+
+/* sum of the CTA partials of the valid [nv][kv] part of the padded [N][K]
+ * tiles: S slices of the CTA list in blockIdx.y, each into tmp[slice][nv*kv + nv] */
+__global__ void k_reduce_parts(int nparts, int N, int K, int nv, int kv, const float *part, const float *bpart,
+                               float *tmp)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x, S = gridDim.y, sl = blockIdx.y;
+	const int per = (nparts + S - 1) / S, c0 = sl * per, c1 = min(nparts, c0 + per);
+	const int nw = nv * kv;
+	if (e < nw) {
+		const int n = e / kv, k = e - n * kv;
+		float s = 0.f;
+		for (int c = c0; c < c1; c++) s += part[((size_t)c * N + n) * K + k];
+		tmp[(size_t)sl * (nw + nv) + e] = s;
+	} else if (e < nw + nv) {
+		float s = 0.f;
+		for (int c = c0; c < c1; c++) s += bpart[(size_t)c * N + (e - nw)];
+		tmp[(size_t)sl * (nw + nv) + e] = s;
+	}
+}
+
+/* gw[e] += sum of the slices (fixed order); then the bias */
+__global__ void k_reduce_final(int S, int nw, int nv, const float *tmp, float *gw, float *gb)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= nw + nv) return;
 	float s = 0.f;
-	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s += mb[(size_t)G.in_idx[q] * W + k];
+	for (int sl = 0; sl < S; sl++) s += tmp[(size_t)sl * (nw + nv) + e];
+	if (e < nw) gw[e] += s;
+	else gb[e - nw] += s;
+}
+
+/* a_i = sum of the messages relu(Zm) into cell i (fixed CSR order); 4 rows per block */
+__global__ void k_aggregate(Graph G, int B, const float *zm, float *agg)
+{
+	const int r = blockIdx.x * 4 + (threadIdx.x >> 6), k = threadIdx.x & 63;
+	if (r >= B * G.nc) return;
+	const int b = r / G.nc, i = r - b * G.nc;
+	const float *mb = zm + (size_t)b * 2 * G.nf * W;
+	float s = 0.f;
+	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s += fmaxf(mb[(size_t)G.in_idx[q] * W + k], 0.f);
 	agg[(size_t)r * W + k] = s;
 }
 
-/* hn = h + relu(Wu [h, a] + bu) */
-__global__ void __launch_bounds__(GT) k_update(int rows, const float *h, const float *agg, const float *Wu,
-                                               const float *bu, float *hn, float *pre)
+/* dh += the outgoing messages' d[h_src] and the incoming messages' d[h_dst]
+ * columns (dxm row stride ld), per cell in fixed CSR order; 4 rows per block */
+__global__ void k_scatter_msg(Graph G, int B, const float *dxm, int ld, float *dh)
 {
-	extern __shared__ __align__(16) unsigned char smem[];
-	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);
-	__nv_bfloat16 *sB = sA + GR * (KUPD + 8);
-	const int row0 = blockIdx.x * GR;
-	for (int e = threadIdx.x; e < GR * KUPD; e += GT) {
-		const int rr = e / KUPD, k = e - rr * KUPD, r = row0 + rr;
-		float v = 0.f;
-		if (r < rows) v = k < W ? h[(size_t)r * W + k] : agg[(size_t)r * W + k - W];
-		sA[rr * (KUPD + 8) + k] = __float2bfloat16_rn(v);
-	}
-	stage_w<KUPD, W>(Wu, KUPD, W, KUPD, sB);
-	__syncthreads();
-	float c[W / 8][4];
-	tile_mma<KUPD, W>(sA, sB, c);
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	for (int nt = 0; nt < W / 8; nt++)
-		for (int hh = 0; hh < 2; hh++) {
-			const int r = row0 + warp * 16 + g + 8 * hh;
-			if (r >= rows) continue;
-			for (int j = 0; j < 2; j++) {
-				const int n = nt * 8 + 2 * t + j;
-				const float z = c[nt][2 * hh + j] + bu[n];
-				pre[(size_t)r * W + n] = z;
-				hn[(size_t)r * W + n] = h[(size_t)r * W + n] + fmaxf(z, 0.f);
-			}
-		}
+	const int r = blockIdx.x * 4 + (threadIdx.x >> 6), k = threadIdx.x & 63;
+	if (r >= B * G.nc) return;
+	const int b = r / G.nc, i = r - b * G.nc;
+	const float *xb = dxm + (size_t)b * 2 * G.nf * ld;
+	float s = 0.f;
+	for (int q = G.out_ptr[i]; q < G.out_ptr[i + 1]; q++) s += xb[(size_t)G.out_idx[q] * ld + k];
+	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s += xb[(size_t)G.in_idx[q] * ld + W + k];
+	dh[(size_t)r * W + k] += s;
 }
 
-/* y = Wd h + bd (4 outputs) */
-__global__ void __launch_bounds__(GT) k_decode(int rows, const float *h, const float *Wd, const float *bd, float *y)
+/* dh[r][k] += dX[r][k] for k < W (dX row stride ld) */
+__global__ void k_add_cols(size_t rows, const float *src, int lds, float *dst)
 {
-	__shared__ __align__(16) __nv_bfloat16 sA[GR * (W + 8)], sB[NDEC * (W + 8)];
-	const int row0 = blockIdx.x * GR;
-	for (int e = threadIdx.x; e < GR * W; e += GT) {
-		const int rr = e / W, k = e - rr * W, r = row0 + rr;
-		sA[rr * (W + 8) + k] = __float2bfloat16_rn(r < rows ? h[(size_t)r * W + k] : 0.f);
-	}
-	stage_w<W, NDEC>(Wd, W, 4, W, sB);
-	__syncthreads();
-	float c[NDEC / 8][4];
-	tile_mma<W, NDEC>(sA, sB, c);
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	for (int hh = 0; hh < 2; hh++) {
-		const int r = row0 + warp * 16 + g + 8 * hh;
-		if (r >= rows) continue;
-		for (int j = 0; j < 2; j++) {
-			const int n = 2 * t + j;
-			if (n < 4) y[(size_t)r * 4 + n] = c[0][2 * hh + j] + bd[n];
-		}
-	}
+	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= rows * W) return;
+	const size_t r = e / W, k = e - r * W;
+	dst[e] += src[r * lds + k];
 }
 
 /* u = uinf + scale * y (double) */
@@ -302,147 +497,6 @@ __global__ void k_loss(int n, const float *y, const double *target, const float 
 	if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-// ------------------------------- backward kernels -------------------------------
-
-/* dZ = dY * (Z > 0) */
-__global__ void k_relu_back(size_t n, const float *dy, const float *z, float *dz)
-{
-	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-	if (e < n) dz[e] = z[e] > 0.f ? dy[e] : 0.f;
-}
-
-/* dX[r][k] = sum_n dZ[r][n] W[n][k] for k < kout: a GEMM with B = W^T */
-template <int K, int N>
-__global__ void __launch_bounds__(GT) k_back_x(int rows, const float *dz, int ldz, int nz, const float *w, int ldw,
-                                               int kout, float *dx, int ldx)
-{
-	extern __shared__ __align__(16) unsigned char smem[];
-	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);  // [64][K] with K = nz padded
-	__nv_bfloat16 *sB = sA + GR * (K + 8);                         // [N][K]: W^T
-	const int row0 = blockIdx.x * GR;
-	for (int e = threadIdx.x; e < GR * K; e += GT) {
-		const int rr = e / K, k = e - rr * K, r = row0 + rr;
-		sA[rr * (K + 8) + k] = __float2bfloat16_rn((r < rows && k < nz) ? dz[(size_t)r * ldz + k] : 0.f);
-	}
-	for (int e = threadIdx.x; e < N * K; e += GT) {
-		const int n = e / K, k = e - n * K;
-		sB[n * (K + 8) + k] = __float2bfloat16_rn((n < kout && k < nz) ? w[(size_t)k * ldw + n] : 0.f);
-	}
-	__syncthreads();
-	float c[N / 8][4];
-	tile_mma<K, N>(sA, sB, c);
-	tile_store<N>(c, row0, rows, nullptr, dx, ldx, kout, nullptr, 0);
-}
-
-/* partial weight gradients of a 64-row chunk: P[chunk][n][k] = sum_r dZ[r][n] X[r][k]
- * (the rows of X come from a loader, as in the forward pass); db partials too */
-template <int K, int N, class Loader>
-__global__ void __launch_bounds__(GT) k_back_w(int rows, const float *dz, int ldz, int nz, Loader ld, float *part,
-                                               float *bpart)
-{
-	extern __shared__ __align__(16) unsigned char smem[];
-	// A = dZ^T [N rows][64 k], B = X^T [K rows][64 k]
-	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(smem);  // [N][64 + 8]
-	__nv_bfloat16 *sB = sA + N * (GR + 8);                         // [K][64 + 8]
-	const int row0 = blockIdx.x * GR;
-	for (int e = threadIdx.x; e < N * GR; e += GT) {
-		const int n = e / GR, rr = e - n * GR, r = row0 + rr;
-		sA[n * (GR + 8) + rr] = __float2bfloat16_rn((r < rows && n < nz) ? dz[(size_t)r * ldz + n] : 0.f);
-	}
-	for (int e = threadIdx.x; e < K * GR; e += GT) {
-		const int k = e / GR, rr = e - k * GR, r = row0 + rr;
-		sB[k * (GR + 8) + rr] = __float2bfloat16_rn(r < rows ? ld(r, k) : 0.f);
-	}
-	__syncthreads();
-	// each warp: 16 of the N rows (N = 64: 4 warps) x K columns
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-	float c[K / 8][4];
-	for (int nt = 0; nt < K / 8; nt++)
-		for (int q = 0; q < 4; q++) c[nt][q] = 0.f;
-	if (warp * 16 < N) {
-		const __nv_bfloat16 *a0 = sA + (warp * 16 + g) * (GR + 8), *a1 = a0 + 8 * (GR + 8);
-		for (int k0 = 0; k0 < GR; k0 += 16) {
-			unsigned af[4];
-			af[0] = *reinterpret_cast<const unsigned *>(a0 + k0 + 2 * t);
-			af[1] = *reinterpret_cast<const unsigned *>(a1 + k0 + 2 * t);
-			af[2] = *reinterpret_cast<const unsigned *>(a0 + k0 + 8 + 2 * t);
-			af[3] = *reinterpret_cast<const unsigned *>(a1 + k0 + 8 + 2 * t);
-			for (int nt = 0; nt < K / 8; nt++) {
-				const __nv_bfloat16 *bp = sB + (nt * 8 + g) * (GR + 8) + k0 + 2 * t;
-				unsigned bf[2];
-				bf[0] = *reinterpret_cast<const unsigned *>(bp);
-				bf[1] = *reinterpret_cast<const unsigned *>(bp + 8);
-				mma_bf16(c[nt], af, bf);
-			}
-		}
-		float *pc = part + (size_t)blockIdx.x * N * K;
-		for (int nt = 0; nt < K / 8; nt++)
-			for (int hh = 0; hh < 2; hh++)
-				for (int j = 0; j < 2; j++) pc[(size_t)(warp * 16 + g + 8 * hh) * K + nt * 8 + 2 * t + j] = c[nt][2 * hh + j];
-	}
-	// bias partials (fp32, fixed order)
-	for (int n = threadIdx.x; n < N; n += GT) {
-		float s = 0.f;
-		for (int rr = 0; rr < GR; rr++) {
-			const int r = row0 + rr;
-			if (r < rows && n < nz) s += dz[(size_t)r * ldz + n];
-		}
-		bpart[(size_t)blockIdx.x * N + n] = s;
-	}
-}
-
-/* sum of the chunk partials into the gradient (fixed order); only the valid
- * [nv][kv] part of the padded [N][K] tiles, into g with row stride kv */
-__global__ void k_reduce_parts(int nchunks, int N, int K, int nv, int kv, const float *part, const float *bpart,
-                               float *gw, float *gb)
-{
-	const int e = blockIdx.x * blockDim.x + threadIdx.x;
-	if (e < nv * kv) {
-		const int n = e / kv, k = e - n * kv;
-		float s = 0.f;
-		for (int c = 0; c < nchunks; c++) s += part[((size_t)c * N + n) * K + k];
-		gw[e] += s;
-	}
-	if (e < nv) {
-		float s = 0.f;
-		for (int c = 0; c < nchunks; c++) s += bpart[(size_t)c * N + e];
-		gb[e] += s;
-	}
-}
-
-/* dh of the message sources / destinations: per cell, the outgoing messages'
- * d[h_src] columns and the incoming messages' d[h_dst] columns */
-__global__ void k_scatter_msg(Graph G, int B, const float *dxm /*[B*2nf][ld]*/, int ld, float *dh)
-{
-	const int r = blockIdx.x, k = threadIdx.x;
-	const int b = r / G.nc, i = r - b * G.nc;
-	const float *xb = dxm + (size_t)b * 2 * G.nf * ld;
-	float s = 0.f;
-	for (int q = G.out_ptr[i]; q < G.out_ptr[i + 1]; q++) s += xb[(size_t)G.out_idx[q] * ld + k];
-	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s += xb[(size_t)G.in_idx[q] * ld + W + k];
-	dh[(size_t)r * W + k] += s;
-}
-
-/* d(message) = d(aggregate) of its destination */
-__global__ void k_gather_agg(Graph G, int B, const float *dagg /*[B*nc][ld]*/, int ld, float *dmsg)
-{
-	const int r = blockIdx.x, k = threadIdx.x;  // r over B * 2nf messages
-	const int per = 2 * G.nf, b = r / per, mid = r - b * per;
-	int s, d;
-	float4 e;
-	msg_ends(G, mid, s, d, e);
-	dmsg[(size_t)r * W + k] = dagg[((size_t)b * G.nc + d) * ld + W + k];
-}
-
-/* dst[r][k] += src[r][k] for k < W (src row stride lds) */
-__global__ void k_add_cols(size_t rows, const float *src, int lds, float *dst)
-{
-	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-	if (e >= rows * W) return;
-	const size_t r = e / W, k = e - r * W;
-	dst[e] += src[r * lds + k];
-}
-
 /* Adam (Kingma & Ba 2015): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
  * p -= lr mhat / (sqrt(vhat) + eps) */
 __global__ void k_adam(int n, float *p, const float *g, float *m, float *v, float lr, float b1, float b2, float eps,
@@ -455,44 +509,6 @@ __global__ void k_adam(int n, float *p, const float *g, float *m, float *v, floa
 	v[e] = b2 * v[e] + (1.f - b2) * gg * gg;
 	p[e] -= lr * (m[e] / c1) / (sqrtf(v[e] / c2) + eps);
 }
-
-// ------------------------------------ loaders ------------------------------------
-
-struct LoadEnc {
-	Graph G;
-	const float *cond;
-	__device__ float operator()(int r, int k) const
-	{
-		if (k >= 7) return 0.f;
-		const int b = r / G.nc, i = r - b * G.nc;
-		const float4 s = G.xs[i];
-		return k == 0 ? s.x : k == 1 ? s.y : k == 2 ? s.z : k == 3 ? s.w : cond[3 * b + (k - 4)];
-	}
-};
-struct LoadMsg {
-	Graph G;
-	const float *h;
-	__device__ float operator()(int r, int k) const
-	{
-		const int per = 2 * G.nf, b = r / per, mid = r - b * per;
-		int s, d;
-		float4 e;
-		msg_ends(G, mid, s, d, e);
-		const float *hb = h + (size_t)b * G.nc * W;
-		if (k < W) return hb[(size_t)s * W + k];
-		if (k < 2 * W) return hb[(size_t)d * W + k - W];
-		return k == 2 * W ? e.x : k == 2 * W + 1 ? e.y : k == 2 * W + 2 ? e.z : 0.f;
-	}
-};
-struct LoadUpd {
-	const float *h, *agg;
-	__device__ float operator()(int r, int k) const { return k < W ? h[(size_t)r * W + k] : agg[(size_t)r * W + k - W]; }
-};
-struct LoadRows {
-	const float *x;
-	int ld;
-	__device__ float operator()(int r, int k) const { return x[(size_t)r * ld + k]; }
-};
 
 }  // namespace
 }  // namespace fvg
@@ -531,9 +547,9 @@ struct fv_mpnn {
 	float *scale = nullptr;
 	// activations (sized for cap_b members)
 	int cap_b = 0;
-	float *h = nullptr, *zpre = nullptr, *msg = nullptr, *mpre = nullptr, *agg = nullptr, *upre = nullptr;
-	float *y = nullptr, *dy = nullptr, *cond = nullptr, *uinf = nullptr, *t1 = nullptr, *t2 = nullptr, *dh = nullptr;
-	float *dmsg = nullptr, *dxm = nullptr, *part = nullptr, *bpart = nullptr, *lpart = nullptr;
+	float *h = nullptr, *zpre = nullptr, *mpre = nullptr, *agg = nullptr, *upre = nullptr;
+	float *y = nullptr, *dy = nullptr, *cond = nullptr, *uinf = nullptr, *t2 = nullptr, *dh = nullptr;
+	float *dxm = nullptr, *part = nullptr, *bpart = nullptr, *rtmp = nullptr, *lpart = nullptr;
 	std::vector<void *> owned;
 };
 
@@ -547,16 +563,14 @@ cudaError_t mall(fv_mpnn *N, T **p, size_t n)
 	return e;
 }
 
-size_t smem_msg() { return sizeof(__nv_bfloat16) * (GR + W) * (KMSG + 8); }
-size_t smem_upd() { return sizeof(__nv_bfloat16) * (GR + W) * (KUPD + 8); }
 
 cudaError_t ensure_capacity(fv_mpnn *N, int B)
 {
 	if (B <= N->cap_b) return cudaSuccess;
 	// activations are re-allocated for the larger batch
-	for (void *q : {(void *)N->h, (void *)N->zpre, (void *)N->msg, (void *)N->mpre, (void *)N->agg, (void *)N->upre,
-	                (void *)N->y, (void *)N->dy, (void *)N->cond, (void *)N->uinf, (void *)N->t1, (void *)N->t2, (void *)N->dh,
-	                (void *)N->dmsg, (void *)N->dxm, (void *)N->part, (void *)N->bpart, (void *)N->lpart})
+	for (void *q : {(void *)N->h, (void *)N->zpre, (void *)N->mpre, (void *)N->agg, (void *)N->upre,
+	                (void *)N->y, (void *)N->dy, (void *)N->cond, (void *)N->uinf, (void *)N->t2, (void *)N->dh,
+	                (void *)N->dxm, (void *)N->part, (void *)N->bpart, (void *)N->rtmp, (void *)N->lpart})
 		if (q) {
 			cudaFree(q);
 			for (auto &o : N->owned)
@@ -568,7 +582,6 @@ cudaError_t ensure_capacity(fv_mpnn *N, int B)
 	auto al = [&](float **p, size_t n) { if (!e) e = mall(N, p, n); };
 	al(&N->h, (L + 1) * rows_c * W);
 	al(&N->zpre, rows_c * W);
-	al(&N->msg, L * rows_m * W);
 	al(&N->mpre, L * rows_m * W);
 	al(&N->agg, L * rows_c * W);
 	al(&N->upre, L * rows_c * W);
@@ -576,14 +589,12 @@ cudaError_t ensure_capacity(fv_mpnn *N, int B)
 	al(&N->dy, rows_c * 4);
 	al(&N->cond, 3 * (size_t)B);
 	al(&N->uinf, 4 * (size_t)B);
-	al(&N->t1, rows_c * W);
 	al(&N->t2, rows_c * KUPD);
 	al(&N->dh, rows_c * W);
-	al(&N->dmsg, rows_m * W);
-	al(&N->dxm, rows_m * KMSG);
-	const size_t chunks = (std::max(rows_m, rows_c) + GR - 1) / GR;
-	al(&N->part, chunks * (size_t)W * KMSG);
-	al(&N->bpart, chunks * (size_t)W);
+	al(&N->dxm, rows_m * 2 * W);
+	al(&N->part, kWgradCtas * (size_t)W * KMSG);
+	al(&N->bpart, kWgradCtas * (size_t)W);
+	al(&N->rtmp, kReduceSlices * ((size_t)W * KMSG + W));
 	al(&N->lpart, 1024);
 	if (!e) N->cap_b = B;
 	return e;
@@ -604,6 +615,16 @@ void set_conditions(fv_mpnn *N, const fv_physics_cfg *phys, int B, std::vector<f
 }
 
 unsigned nb(size_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+/* persistent GEMM grid: at most 4 CTAs per SM (152 SMs) over the 64-row tiles */
+unsigned gemm_grid(size_t rows) { return std::min<unsigned>(nb(rows, GR), 4 * 152); }
+
+/* Z = A W^T (or A W with TRANS) over rows, epilogue ep */
+template <int K, int Nn, bool TRANS, class L, class E>
+void gemm(size_t rows, L ld, const float *w, int ldw, int nvalid, int kvalid, E ep, cudaStream_t s)
+{
+	const size_t sm = sizeof(__nv_bfloat16) * (GR + Nn) * (K + 8);
+	k_gemm<K, Nn, TRANS, L, E><<<gemm_grid(rows), GT, sm, s>>>((int)rows, ld, w, ldw, nvalid, kvalid, ep);
+}
 
 /* forward pass for B members; activations kept for the backward pass */
 cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
@@ -612,31 +633,36 @@ cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
 	const MpnnLayout &Y = N->lay;
 	const float *P = N->p;
 	const size_t nc = G.nc, nm = 2 * (size_t)G.nf, rows_c = B * nc, rows_m = B * nm;
-	k_encode<<<nb(rows_c, GR), GT, 0, s>>>(G, B, N->cond, P + Y.we, P + Y.be, N->h, N->zpre);
+	gemm<KENC, W, false>(rows_c, LEnc{G, N->cond}, P + Y.we, 7, W, 7, EStore{P + Y.be, N->h, N->zpre, W, W, 1}, s);
 	for (int l = 0; l < Y.layers; l++) {
 		const float *hl = N->h + l * rows_c * W;
-		float *ml = N->msg + l * rows_m * W, *mp = N->mpre + l * rows_m * W;
-		k_message<<<nb(rows_m, GR), GT, smem_msg(), s>>>(G, B, hl, P + Y.wm[l], P + Y.bm[l], ml, mp);
+		float *mp = N->mpre + l * rows_m * W;  // Zm; the messages relu(Zm) are not stored
+		gemm<KMSG, W, false>(rows_m, LMsg{G, hl}, P + Y.wm[l], 2 * W + 3, W, 2 * W + 3,
+		                     EStore{P + Y.bm[l], mp, nullptr, W, W, 0}, s);
 		float *al = N->agg + l * rows_c * W;
-		k_aggregate<<<(unsigned)rows_c, W, 0, s>>>(G, B, ml, al);
-		k_update<<<nb(rows_c, GR), GT, smem_upd(), s>>>((int)rows_c, hl, al, P + Y.wu[l], P + Y.bu[l],
-		                                                N->h + (l + 1) * rows_c * W, N->upre + l * rows_c * W);
+		k_aggregate<<<nb(rows_c, 4), 256, 0, s>>>(G, B, mp, al);
+		gemm<KUPD, W, false>(rows_c, LUpd{hl, al}, P + Y.wu[l], KUPD, W, KUPD,
+		                     EUpdate{P + Y.bu[l], hl, N->h + (l + 1) * rows_c * W, N->upre + l * rows_c * W}, s);
 	}
-	k_decode<<<nb(rows_c, GR), GT, 0, s>>>((int)rows_c, N->h + Y.layers * rows_c * W, P + Y.wd, P + Y.bd, N->y);
+	gemm<W, NDEC, false>(rows_c, LRows{N->h + Y.layers * rows_c * W, W, W}, P + Y.wd, W, 4, W,
+	                     EStore{P + Y.bd, N->y, nullptr, 4, 4, 0}, s);
 	count_launches(2 + 3 * Y.layers);
 	return cudaGetLastError();
 }
 
-template <int K, int Nn, class Loader>
-cudaError_t weight_grad(int rows, const float *dz, int ldz, int nz, Loader ld, float *part, float *bpart, int nv,
-                        int kv, float *gw, float *gb, cudaStream_t s)
+/* weight and bias gradients of one layer: CTA partials, then a sliced
+ * fixed-order reduction into gw [nv][kv] and gb [nv] (accumulated) */
+template <int K, int Nn, class XL, class ZL>
+void wgrad(fv_mpnn *N, size_t rows, XL xl, ZL zl, int nv, int kv, float *gw, float *gb, cudaStream_t s)
 {
-	const unsigned chunks = nb(rows, GR);
-	const size_t sm = sizeof(__nv_bfloat16) * (Nn + K) * (GR + 8);
-	k_back_w<K, Nn, Loader><<<chunks, GT, sm, s>>>(rows, dz, ldz, nz, ld, part, bpart);
-	k_reduce_parts<<<nb((size_t)nv * kv, 256), 256, 0, s>>>((int)chunks, Nn, K, nv, kv, part, bpart, gw, gb);
-	count_launches(2);
-	return cudaGetLastError();
+	const unsigned ctas = std::min<unsigned>(nb(rows, GR), kWgradCtas);
+	const size_t sm = sizeof(__nv_bfloat16) * GR * (Nn + 8 + K + 8);
+	k_wgrad<K, Nn, XL, ZL><<<ctas, GT, sm, s>>>((int)rows, xl, zl, N->part, N->bpart);
+	const int nw = nv * kv;
+	k_reduce_parts<<<dim3(nb(nw + nv, 256), kReduceSlices), 256, 0, s>>>((int)ctas, Nn, K, nv, kv, N->part, N->bpart,
+	                                                                   N->rtmp);
+	k_reduce_final<<<nb(nw + nv, 256), 256, 0, s>>>(kReduceSlices, nw, nv, N->rtmp, gw, gb);
+	count_launches(3);
 }
 
 /* backward pass from N->dy; gradients accumulate into N->g */
@@ -648,37 +674,30 @@ cudaError_t backward(fv_mpnn *N, int B, cudaStream_t s)
 	float *Gr = N->g;
 	const size_t nc = G.nc, nm = 2 * (size_t)G.nf, rows_c = B * nc, rows_m = B * nm;
 	const float *hL = N->h + Y.layers * rows_c * W;
-	// decoder: y = Wd h + bd
-	weight_grad<W, 16>((int)rows_c, N->dy, 4, 4, LoadRows{hL, W}, N->part, N->bpart, 4, W, Gr + Y.wd, Gr + Y.bd, s);
-	k_back_x<16, W><<<nb(rows_c, GR), GT, sizeof(__nv_bfloat16) * (GR + W) * (16 + 8), s>>>(
-	    (int)rows_c, N->dy, 4, 4, P + Y.wd, W, W, N->dh, W);
+	// decoder: y = Wd h + bd;  dh = dy Wd
+	wgrad<W, 16>(N, rows_c, LRows{hL, W, W}, LRows{N->dy, 4, 4}, 4, W, Gr + Y.wd, Gr + Y.bd, s);
+	gemm<16, W, true>(rows_c, LRows{N->dy, 4, 4}, P + Y.wd, W, W, 4, EStore{nullptr, N->dh, nullptr, W, W, 0}, s);
 	count_launches(1);
 	for (int l = Y.layers - 1; l >= 0; l--) {
 		const float *hl = N->h + l * rows_c * W;
 		const float *al = N->agg + l * rows_c * W;
-		// update: hn = h + relu(Zu), Zu = Wu [h, a] + bu
-		k_relu_back<<<nb(rows_c * W, 256), 256, 0, s>>>(rows_c * W, N->dh, N->upre + l * rows_c * W, N->t1);
-		weight_grad<KUPD, W>((int)rows_c, N->t1, W, W, LoadUpd{hl, al}, N->part, N->bpart, W, KUPD, Gr + Y.wu[l],
-		                     Gr + Y.bu[l], s);
-		k_back_x<W, KUPD><<<nb(rows_c, GR), GT, sizeof(__nv_bfloat16) * (GR + KUPD) * (W + 8), s>>>(
-		    (int)rows_c, N->t1, W, W, P + Y.wu[l], KUPD, KUPD, N->t2, KUPD);
-		// residual path and the update's d[h] columns
+		const float *up = N->upre + l * rows_c * W, *mp = N->mpre + l * rows_m * W;
+		// update: hn = h + relu(Zu), Zu = Wu [h, a] + bu;  dZu = dh (Zu > 0)
+		wgrad<KUPD, W>(N, rows_c, LUpd{hl, al}, LRelu{N->dh, up}, W, KUPD, Gr + Y.wu[l], Gr + Y.bu[l], s);
+		gemm<W, KUPD, true>(rows_c, LRelu{N->dh, up}, P + Y.wu[l], KUPD, KUPD, W,
+		                    EStore{nullptr, N->t2, nullptr, KUPD, KUPD, 0}, s);
+		// residual path plus the update's d[h] columns
 		k_add_cols<<<nb(rows_c * W, 256), 256, 0, s>>>(rows_c, N->t2, KUPD, N->dh);
-		// messages: dm = d[a] of the destination, dZm = dm (Zm > 0)
-		k_gather_agg<<<(unsigned)rows_m, W, 0, s>>>(G, B, N->t2, KUPD, N->dmsg);
-		k_relu_back<<<nb(rows_m * W, 256), 256, 0, s>>>(rows_m * W, N->dmsg, N->mpre + l * rows_m * W, N->dmsg);
-		weight_grad<KMSG, W>((int)rows_m, N->dmsg, W, W, LoadMsg{G, hl}, N->part, N->bpart, W, 2 * W + 3,
-		                     Gr + Y.wm[l], Gr + Y.bm[l], s);
-		k_back_x<W, KMSG><<<nb(rows_m, GR), GT, sizeof(__nv_bfloat16) * (GR + KMSG) * (W + 8), s>>>(
-		    (int)rows_m, N->dmsg, W, W, P + Y.wm[l], 2 * W + 3, 2 * W, N->dxm, KMSG);
-		k_scatter_msg<<<(unsigned)rows_c, W, 0, s>>>(G, B, N->dxm, KMSG, N->dh);
-		count_launches(7);
+		// messages: dZm = d[a] of the destination, masked by Zm > 0
+		const LMsgGrad dzm{G, N->t2, KUPD, W, mp};
+		wgrad<KMSG, W>(N, rows_m, LMsg{G, hl}, dzm, W, 2 * W + 3, Gr + Y.wm[l], Gr + Y.bm[l], s);
+		gemm<W, 2 * W, true>(rows_m, dzm, P + Y.wm[l], 2 * W + 3, 2 * W, W,
+		                     EStore{nullptr, N->dxm, nullptr, 2 * W, 2 * W, 0}, s);
+		k_scatter_msg<<<nb(rows_c, 4), 256, 0, s>>>(G, B, N->dxm, 2 * W, N->dh);
+		count_launches(4);
 	}
 	// encoder: h0 = relu(We x + be)
-	k_relu_back<<<nb(rows_c * W, 256), 256, 0, s>>>(rows_c * W, N->dh, N->zpre, N->t1);
-	weight_grad<KENC, W>((int)rows_c, N->t1, W, W, LoadEnc{G, N->cond}, N->part, N->bpart, W, 7, Gr + Y.we,
-	                     Gr + Y.be, s);
-	count_launches(1);
+	wgrad<KENC, W>(N, rows_c, LEnc{G, N->cond}, LRelu{N->dh, N->zpre}, W, 7, Gr + Y.we, Gr + Y.be, s);
 	return cudaGetLastError();
 }
 

@@ -58,3 +58,23 @@ RESIDUAL_CASES = [
      dict(flux="HLLC"), [(1, "slipwall", ()), (2, "extrapolation", ()), (3, "slipwall", ()),
                          (4, "subsonic_inflow", (1.0 / (1.4 * 0.16) * 1.1, 288.15 * 1.032))]),
 ]
+
+
+def write_gmsh(m, path):
+    """Writes a mesh as Gmsh 2.2 ASCII (boundary faces as lines with their
+    markers as physical tags, cells as triangles / quads)."""
+    ex = m.export()
+    with open(path, "w") as f:
+        f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$Nodes\n%d\n" % len(ex["coords"]))
+        for k, (x, y) in enumerate(ex["coords"]):
+            f.write("%d %.17g %.17g 0\n" % (k + 1, x, y))
+        nb, ne = len(ex["btag"]), len(ex["nnode"])
+        f.write("$EndNodes\n$Elements\n%d\n" % (nb + ne))
+        k = 1
+        for (a, b), t in zip(ex["bface"], ex["btag"]):
+            f.write("%d 1 2 %d %d %d %d\n" % (k, t, t, a + 1, b + 1))
+            k += 1
+        for nn, nodes in zip(ex["nnode"], ex["inpoel"]):
+            f.write("%d %d 2 0 1 %s\n" % (k, 2 if nn == 3 else 3, " ".join(str(v + 1) for v in nodes[:nn])))
+            k += 1
+        f.write("$EndElements\n")
