@@ -297,11 +297,12 @@ __global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, 
  * before the whole part) or untouched until a later one.  Phase 1 (all PT
  * threads, one cell each) therefore does all the work that involves
  * neighbours outside the part -- in parallel, with the part's own blocks
- * copied to shared memory; phase 2 (warp 0, four lanes per cell, one block
- * row each) walks the part's dependency levels reading shared memory only;
- * phase 3 (all threads) writes the part back.  The dependency chain of a part
- * thus costs shared-memory latency per level. */
-constexpr int PT = 128;  // threads per part CTA; warp 0 walks the levels (8 cells x 4 block rows per pass)
+ * copied to shared memory; phase 2 (all threads, four lanes per cell, one
+ * block row each, a CTA barrier between levels) walks the part's dependency
+ * levels reading shared memory only; phase 3 (all threads) writes the part
+ * back.  The dependency chain of a part thus costs shared-memory latency and
+ * one barrier per level. */
+constexpr int PT = 128;  // threads per part CTA (32 cells x 4 block rows per pass of a level)
 
 /* dynamic shared memory of the sweep kernels for parts of at most cap cells */
 template <class R>
@@ -368,13 +369,12 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 		}
 	}
 	__syncthreads();
-	if (threadIdx.x < 32) {
-		const int lane = threadIdx.x;
+	{
 		const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-		const int g = lane >> 2, row = lane & 3;
+		const int g = threadIdx.x >> 2, row = threadIdx.x & 3;
 		for (int l = l0; l < l1; l++) {
 			const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
-			for (int c0 = ls; c0 < le; c0 += 8) {
+			for (int c0 = ls; c0 < le; c0 += PT / 4) {
 				const int c = c0 + g;
 				const bool on = c < le;
 				R acc = R(0);
@@ -392,10 +392,9 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 				}
 				if (on) sv[4 * c + row] = acc;
 			}
-			__syncwarp();
+			__syncthreads();  // the level's values are read by the next level
 		}
 	}
-	__syncthreads();
 	for (int e = threadIdx.x; e < 4 * n; e += PT) yb[(size_t)p0 * 4 + e] = sv[e];
 }
 
@@ -457,13 +456,12 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 		store_blk(sD + (size_t)c * 16, d);
 	}
 	__syncthreads();
-	if (threadIdx.x < 32) {
-		const int lane = threadIdx.x;
+	{
 		const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-		const int g = lane >> 2, row = lane & 3;
+		const int g = threadIdx.x >> 2, row = threadIdx.x & 3;
 		for (int l = l1 - 1; l >= l0; l--) {
 			const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
-			for (int c0 = ls; c0 < le; c0 += 8) {
+			for (int c0 = ls; c0 < le; c0 += PT / 4) {
 				const int c = c0 + g;
 				const bool on = c < le;
 				if (on) {
@@ -481,10 +479,9 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 					sv[4 * c + row] = sgs ? sv[4 * c + row] - dz : dz;
 				}
 			}
-			__syncwarp();
+			__syncthreads();  // the level's values are read by the next level
 		}
 	}
-	__syncthreads();
 	for (int c = threadIdx.x; c < n; c += PT) {
 		const R *v = sv + 4 * c;
 		reinterpret_cast<double4 *>(zb)[pos_cell[p0 + c]] = make_double4(double(v[0]), double(v[1]), double(v[2]), double(v[3]));

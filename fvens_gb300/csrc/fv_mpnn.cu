@@ -17,11 +17,18 @@
  * y is the state's deviation from freestream, per variable over a scale the
  * caller sets (fv_mpnn_set_scale).
  *
+ * The message MLP's first layer is linear in h_s and h_d, so it runs per
+ * cell: pc = [W_s h, W_d h] (one GEMM over cells), and per message
+ * Zm = pc_s[s] + pc_d[d] + W_e e_sd + bm (a gather, no GEMM over messages).
+ * Its backward pass likewise sums dZm per cell over outgoing and incoming
+ * messages (S_out, S_in) and forms the weight and input gradients with GEMMs
+ * over cells; the edge weights' gradient and the bias sum over messages.
+ *
  * Arithmetic: every contraction runs on the tensor cores as warp-level BF16
  * mma.sync (m16n8k16) with FP32 accumulation: GEMM operands (weights and
- * activations) are rounded to BF16 when they are staged in shared memory;
+ * activations, S) are rounded to BF16 when they are staged in shared memory;
  * activations, biases, gradients and the Adam state stay FP32.  The GEMMs are
- * small (K <= 144, N = 64), far from the solver's hot path.
+ * small (K <= 128, N <= 128), far from the solver's hot path.
  * Reductions over rows (weight gradients, aggregation) run in fixed order.
  */
 #include <cuda_bf16.h>
@@ -39,13 +46,13 @@ namespace {
 
 constexpr int W = 64;        // width
 constexpr int KENC = 16;     // encoder inputs, padded
-constexpr int KMSG = 144;    // message inputs 64 + 64 + 3, padded
 constexpr int KUPD = 128;    // update inputs
 constexpr int NDEC = 8;      // decoder outputs 4, padded
 constexpr int GT = 128;      // GEMM CTA threads (4 warps x 16 rows)
 constexpr int GR = 64;       // GEMM rows per CTA
 constexpr int kWgradCtas = 608;  // weight-gradient CTAs (4 per SM of 152), each over many row chunks
 constexpr int kReduceSlices = 16;  // slices of the CTA partials in the gradient reduction
+constexpr int kMsgBackBlocks = 1216;  // blocks of the message-layer backward (8 per SM of 152)
 
 __device__ __forceinline__ unsigned pack_bf16(float lo, float hi)
 {
@@ -168,24 +175,6 @@ struct LEnc {  // [xs (4), M, AoA, Re (3), 0...]: K = 16
 		return make_float4(0.f, 0.f, 0.f, 0.f);
 	}
 };
-struct LMsg {  // [h_src (64), h_dst (64), e (3), 0...]: K = 144
-	Graph G;
-	const float *h;
-	__device__ void prep(int r, RowInfo &ri) const
-	{
-		const int per = 2 * G.nf, b = r / per;
-		msg_ends(G, r - b * per, ri.src, ri.dst, ri.e);
-		ri.src += b * G.nc;
-		ri.dst += b * G.nc;
-	}
-	__device__ float4 quad(int, const RowInfo &ri, int q) const
-	{
-		if (q < W / 4) return reinterpret_cast<const float4 *>(h + (size_t)ri.src * W)[q];
-		if (q < W / 2) return reinterpret_cast<const float4 *>(h + (size_t)ri.dst * W)[q - W / 4];
-		if (q == W / 2) return make_float4(ri.e.x, ri.e.y, ri.e.z, 0.f);
-		return make_float4(0.f, 0.f, 0.f, 0.f);
-	}
-};
 struct LUpd {  // [h (64), a (64)]: K = 128
 	const float *h, *agg;
 	__device__ void prep(int, RowInfo &) const {}
@@ -215,26 +204,6 @@ struct LRelu {  // dZ = dY (Z > 0), rows of width 64
 		                   zz.w > 0.f ? d.w : 0.f);
 	}
 };
-struct LMsgGrad {  // dZm = d(aggregate) of the destination, masked by Zm > 0
-	Graph G;
-	const float *dagg;  // [B*nc][lda], the aggregate's columns from off
-	int lda, off;
-	const float *z;     // Zm [B*2nf][64]
-	__device__ void prep(int r, RowInfo &ri) const
-	{
-		const int per = 2 * G.nf, b = r / per;
-		msg_ends(G, r - b * per, ri.src, ri.dst, ri.e);
-		ri.dst += b * G.nc;
-	}
-	__device__ float4 quad(int r, const RowInfo &ri, int q) const
-	{
-		const float4 d = reinterpret_cast<const float4 *>(dagg + (size_t)ri.dst * lda + off)[q];
-		const float4 zz = reinterpret_cast<const float4 *>(z + (size_t)r * W)[q];
-		return make_float4(zz.x > 0.f ? d.x : 0.f, zz.y > 0.f ? d.y : 0.f, zz.z > 0.f ? d.z : 0.f,
-		                   zz.w > 0.f ? d.w : 0.f);
-	}
-};
-
 /* stages the rows of a 64-row tile as bf16 [64][K + 8] (8-byte stores) */
 template <int K, class L>
 __device__ __forceinline__ void stage_rows(const L &ld, int row0, int rows, RowInfo *ri, __nv_bfloat16 *sA)
@@ -271,6 +240,17 @@ struct EUpdate {  // hn = h + relu(Z + bu), pre = Z + bu
 		const float2 hh = *reinterpret_cast<const float2 *>(h + (size_t)r * W + n);
 		*reinterpret_cast<float2 *>(pre + (size_t)r * W + n) = v;
 		*reinterpret_cast<float2 *>(hn + (size_t)r * W + n) = make_float2(hh.x + fmaxf(v.x, 0.f), hh.y + fmaxf(v.y, 0.f));
+	}
+};
+
+struct EAccum {  // out += Z (row stride ldo)
+	float *out;
+	int ldo;
+	__device__ void operator()(int r, int n, float z0, float z1) const
+	{
+		float2 *o = reinterpret_cast<float2 *>(out + (size_t)r * ldo + n);
+		const float2 v = *o;
+		*o = make_float2(v.x + z0, v.y + z1);
 	}
 };
 
@@ -418,15 +398,23 @@ __global__ void k_reduce_parts(int nparts, int N, int K, int nv, int kv, const f
 	}
 }
 
-/* gw[e] += sum of the slices (fixed order); then the bias */
-__global__ void k_reduce_final(int S, int nw, int nv, const float *tmp, float *gw, float *gb)
+/* gw[e] += sum of the slices (fixed order); then the bias (gb may be null).
+ * stacked: the partial is P[n][k] = sum_r h[r][n] [S_out, S_in][r][k] of a
+ * message layer (nv = 64, kv = 128), added to the message weights' gradient
+ * at row k mod 64, column (k / 64) * 64 + n (row stride ldg). */
+__global__ void k_reduce_final(int S, int nw, int nv, int kv, const float *tmp, float *gw, float *gb, int stacked,
+                               int ldg)
 {
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
-	if (e >= nw + nv) return;
+	if (e >= nw + nv || (e >= nw && !gb)) return;
 	float s = 0.f;
 	for (int sl = 0; sl < S; sl++) s += tmp[(size_t)sl * (nw + nv) + e];
-	if (e < nw) gw[e] += s;
-	else gb[e - nw] += s;
+	if (e >= nw) gb[e - nw] += s;
+	else if (!stacked) gw[e] += s;
+	else {
+		const int n = e / kv, k = e - n * kv;
+		gw[(size_t)(k % W) * ldg + (k / W) * W + n] += s;
+	}
 }
 
 /* a_i = sum of the messages relu(Zm) into cell i (fixed CSR order); 4 rows per block */
@@ -441,18 +429,97 @@ __global__ void k_aggregate(Graph G, int B, const float *zm, float *agg)
 	agg[(size_t)r * W + k] = s;
 }
 
-/* dh += the outgoing messages' d[h_src] and the incoming messages' d[h_dst]
- * columns (dxm row stride ld), per cell in fixed CSR order; 4 rows per block */
-__global__ void k_scatter_msg(Graph G, int B, const float *dxm, int ld, float *dh)
+/* Wst [128][64]: rows 0..63 the message weights' h_src block W_s, rows
+ * 64..127 the h_dst block W_d (Wm row stride 2 W + 3) */
+__global__ void k_stack_w(const float *wm, float *wst)
 {
-	const int r = blockIdx.x * 4 + (threadIdx.x >> 6), k = threadIdx.x & 63;
-	if (r >= B * G.nc) return;
-	const int b = r / G.nc, i = r - b * G.nc;
-	const float *xb = dxm + (size_t)b * 2 * G.nf * ld;
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if (e >= 2 * W * W) return;
+	const int n = e / W, k = e - n * W;
+	wst[e] = wm[(size_t)(n % W) * (2 * W + 3) + (n / W) * W + k];
+}
+
+/* Zm = W_s h_src + W_d h_dst + W_e e + bm from the per-cell projections
+ * pc = [W_s h, W_d h] (row stride 2 W); the edge term with BF16-rounded W_e and
+ * e, as the GEMM operands.  4 messages x 64 columns per block. */
+__global__ void k_msg_fwd(Graph G, int B, const float *pc, const float *wm, const float *bm, float *zm)
+{
+	const int r = blockIdx.x * 4 + (threadIdx.x >> 6), n = threadIdx.x & 63;
+	const int per = 2 * G.nf;
+	if (r >= B * per) return;
+	const int b = r / per;
+	int src, dst;
+	float4 e;
+	msg_ends(G, r - b * per, src, dst, e);
+	const size_t cs = (size_t)b * G.nc + src, cd = (size_t)b * G.nc + dst;
+	const float *we = wm + (size_t)n * (2 * W + 3) + 2 * W;
+	const float bfe = __bfloat162float(__float2bfloat16_rn(e.x)) * __bfloat162float(__float2bfloat16_rn(we[0])) +
+	                  __bfloat162float(__float2bfloat16_rn(e.y)) * __bfloat162float(__float2bfloat16_rn(we[1])) +
+	                  __bfloat162float(__float2bfloat16_rn(e.z)) * __bfloat162float(__float2bfloat16_rn(we[2]));
+	zm[(size_t)r * W + n] = pc[cs * 2 * W + n] + pc[cd * 2 * W + W + n] + bfe + bm[n];
+}
+
+/* Message-layer backward from da (the aggregate's gradient, columns off.. of
+ * rows with stride lda): per cell the sums of dZm = da[dst] (Zm > 0) over its
+ * outgoing and incoming messages, S = [S_out, S_in] (row stride 2 W); and the
+ * edge-weight and bias gradients sum_m dZm e_m, sum_m dZm accumulated over
+ * each cell's incoming messages (every message once), per thread in fixed
+ * order over the cells it visits, then per block in fixed order into
+ * epart[block][64][4].  4 cells x 64 columns per block, grid-stride over cells. */
+__global__ void k_msg_back(Graph G, int B, const float *zm, const float *dagg, int lda, int off, float *S,
+                           float *epart)
+{
+	const int n = threadIdx.x & 63, slot = threadIdx.x >> 6;
+	const int rows = B * G.nc;
+	const size_t per = 2 * (size_t)G.nf;
+	float ae[4] = {0.f, 0.f, 0.f, 0.f};
+	for (int r = blockIdx.x * 4 + slot; r < rows; r += gridDim.x * 4) {
+		const int b = r / G.nc, i = r - b * G.nc;
+		const float *zb = zm + (size_t)b * per * W;
+		const float di = dagg[(size_t)r * lda + off + n];
+		float sin_ = 0.f, sout = 0.f;
+		for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) {
+			const int m = G.in_idx[q];
+			const float dz = zb[(size_t)m * W + n] > 0.f ? di : 0.f;
+			sin_ += dz;
+			int s0, d0;
+			float4 e;
+			msg_ends(G, m, s0, d0, e);
+			ae[0] += dz * __bfloat162float(__float2bfloat16_rn(e.x));
+			ae[1] += dz * __bfloat162float(__float2bfloat16_rn(e.y));
+			ae[2] += dz * __bfloat162float(__float2bfloat16_rn(e.z));
+			ae[3] += dz;
+		}
+		for (int q = G.out_ptr[i]; q < G.out_ptr[i + 1]; q++) {
+			const int m = G.out_idx[q];
+			int s0, d0;
+			float4 e;
+			msg_ends(G, m, s0, d0, e);
+			const float dd = dagg[((size_t)b * G.nc + d0) * lda + off + n];
+			sout += zb[(size_t)m * W + n] > 0.f ? dd : 0.f;
+		}
+		S[(size_t)r * 2 * W + n] = sout;
+		S[(size_t)r * 2 * W + W + n] = sin_;
+	}
+	__shared__ float sh[4][64][4];
+	for (int k = 0; k < 4; k++) sh[slot][n][k] = ae[k];
+	__syncthreads();
+	if (threadIdx.x < 64)
+		for (int k = 0; k < 4; k++)
+			epart[((size_t)blockIdx.x * 64 + n) * 4 + k] = sh[0][n][k] + sh[1][n][k] + sh[2][n][k] + sh[3][n][k];
+}
+
+/* edge-weight columns and bias of a message layer's gradient: sum of the
+ * block partials in fixed order */
+__global__ void k_reduce_edge(int nblk, const float *epart, float *gwm, float *gbm)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;  // (n, k), k < 4
+	if (e >= 64 * 4) return;
+	const int n = e >> 2, k = e & 3;
 	float s = 0.f;
-	for (int q = G.out_ptr[i]; q < G.out_ptr[i + 1]; q++) s += xb[(size_t)G.out_idx[q] * ld + k];
-	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s += xb[(size_t)G.in_idx[q] * ld + W + k];
-	dh[(size_t)r * W + k] += s;
+	for (int c = 0; c < nblk; c++) s += epart[((size_t)c * 64 + n) * 4 + k];
+	if (k < 3) gwm[(size_t)n * (2 * W + 3) + 2 * W + k] += s;
+	else gbm[n] += s;
 }
 
 /* dh[r][k] += dX[r][k] for k < W (dX row stride ld) */
@@ -549,7 +616,8 @@ struct fv_mpnn {
 	int cap_b = 0;
 	float *h = nullptr, *zpre = nullptr, *mpre = nullptr, *agg = nullptr, *upre = nullptr;
 	float *y = nullptr, *dy = nullptr, *cond = nullptr, *uinf = nullptr, *t2 = nullptr, *dh = nullptr;
-	float *dxm = nullptr, *part = nullptr, *bpart = nullptr, *rtmp = nullptr, *lpart = nullptr;
+	float *pc = nullptr, *sgrad = nullptr, *wst = nullptr, *epart = nullptr;
+	float *part = nullptr, *bpart = nullptr, *rtmp = nullptr, *lpart = nullptr;
 	std::vector<void *> owned;
 };
 
@@ -570,7 +638,8 @@ cudaError_t ensure_capacity(fv_mpnn *N, int B)
 	// activations are re-allocated for the larger batch
 	for (void *q : {(void *)N->h, (void *)N->zpre, (void *)N->mpre, (void *)N->agg, (void *)N->upre,
 	                (void *)N->y, (void *)N->dy, (void *)N->cond, (void *)N->uinf, (void *)N->t2, (void *)N->dh,
-	                (void *)N->dxm, (void *)N->part, (void *)N->bpart, (void *)N->rtmp, (void *)N->lpart})
+	                (void *)N->pc, (void *)N->sgrad, (void *)N->wst, (void *)N->epart, (void *)N->part,
+	                (void *)N->bpart, (void *)N->rtmp, (void *)N->lpart})
 		if (q) {
 			cudaFree(q);
 			for (auto &o : N->owned)
@@ -591,10 +660,13 @@ cudaError_t ensure_capacity(fv_mpnn *N, int B)
 	al(&N->uinf, 4 * (size_t)B);
 	al(&N->t2, rows_c * KUPD);
 	al(&N->dh, rows_c * W);
-	al(&N->dxm, rows_m * 2 * W);
-	al(&N->part, kWgradCtas * (size_t)W * KMSG);
+	al(&N->pc, rows_c * 2 * W);
+	al(&N->sgrad, rows_c * 2 * W);
+	al(&N->wst, L * 2 * W * W);
+	al(&N->epart, (size_t)kMsgBackBlocks * W * 4);
+	al(&N->part, kWgradCtas * (size_t)W * 2 * W);
 	al(&N->bpart, kWgradCtas * (size_t)W);
-	al(&N->rtmp, kReduceSlices * ((size_t)W * KMSG + W));
+	al(&N->rtmp, kReduceSlices * ((size_t)W * 2 * W + W));
 	al(&N->lpart, 1024);
 	if (!e) N->cap_b = B;
 	return e;
@@ -637,8 +709,13 @@ cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
 	for (int l = 0; l < Y.layers; l++) {
 		const float *hl = N->h + l * rows_c * W;
 		float *mp = N->mpre + l * rows_m * W;  // Zm; the messages relu(Zm) are not stored
-		gemm<KMSG, W, false>(rows_m, LMsg{G, hl}, P + Y.wm[l], 2 * W + 3, W, 2 * W + 3,
-		                     EStore{P + Y.bm[l], mp, nullptr, W, W, 0}, s);
+		// the message MLP's first layer per cell: pc = [W_s h, W_d h], then per message
+		// Zm = pc_s[src] + pc_d[dst] + W_e e + bm
+		float *wst = N->wst + (size_t)l * 2 * W * W;
+		k_stack_w<<<nb(2 * W * W, 256), 256, 0, s>>>(P + Y.wm[l], wst);
+		gemm<W, 2 * W, false>(rows_c, LRows{hl, W, W}, wst, W, 2 * W, W, EStore{nullptr, N->pc, nullptr, 2 * W, 2 * W, 0},
+		                      s);
+		k_msg_fwd<<<nb(rows_m, 4), 256, 0, s>>>(G, B, N->pc, P + Y.wm[l], P + Y.bm[l], mp);
 		float *al = N->agg + l * rows_c * W;
 		k_aggregate<<<nb(rows_c, 4), 256, 0, s>>>(G, B, mp, al);
 		gemm<KUPD, W, false>(rows_c, LUpd{hl, al}, P + Y.wu[l], KUPD, W, KUPD,
@@ -646,14 +723,15 @@ cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
 	}
 	gemm<W, NDEC, false>(rows_c, LRows{N->h + Y.layers * rows_c * W, W, W}, P + Y.wd, W, 4, W,
 	                     EStore{P + Y.bd, N->y, nullptr, 4, 4, 0}, s);
-	count_launches(2 + 3 * Y.layers);
+	count_launches(2 + 5 * Y.layers);
 	return cudaGetLastError();
 }
 
 /* weight and bias gradients of one layer: CTA partials, then a sliced
  * fixed-order reduction into gw [nv][kv] and gb [nv] (accumulated) */
 template <int K, int Nn, class XL, class ZL>
-void wgrad(fv_mpnn *N, size_t rows, XL xl, ZL zl, int nv, int kv, float *gw, float *gb, cudaStream_t s)
+void wgrad(fv_mpnn *N, size_t rows, XL xl, ZL zl, int nv, int kv, float *gw, float *gb, cudaStream_t s,
+           int stacked = 0)
 {
 	const unsigned ctas = std::min<unsigned>(nb(rows, GR), kWgradCtas);
 	const size_t sm = sizeof(__nv_bfloat16) * GR * (Nn + 8 + K + 8);
@@ -661,7 +739,7 @@ void wgrad(fv_mpnn *N, size_t rows, XL xl, ZL zl, int nv, int kv, float *gw, flo
 	const int nw = nv * kv;
 	k_reduce_parts<<<dim3(nb(nw + nv, 256), kReduceSlices), 256, 0, s>>>((int)ctas, Nn, K, nv, kv, N->part, N->bpart,
 	                                                                   N->rtmp);
-	k_reduce_final<<<nb(nw + nv, 256), 256, 0, s>>>(kReduceSlices, nw, nv, N->rtmp, gw, gb);
+	k_reduce_final<<<nb(nw + nv, 256), 256, 0, s>>>(kReduceSlices, nw, nv, kv, N->rtmp, gw, gb, stacked, 2 * W + 3);
 	count_launches(3);
 }
 
@@ -688,12 +766,16 @@ cudaError_t backward(fv_mpnn *N, int B, cudaStream_t s)
 		                    EStore{nullptr, N->t2, nullptr, KUPD, KUPD, 0}, s);
 		// residual path plus the update's d[h] columns
 		k_add_cols<<<nb(rows_c * W, 256), 256, 0, s>>>(rows_c, N->t2, KUPD, N->dh);
-		// messages: dZm = d[a] of the destination, masked by Zm > 0
-		const LMsgGrad dzm{G, N->t2, KUPD, W, mp};
-		wgrad<KMSG, W>(N, rows_m, LMsg{G, hl}, dzm, W, 2 * W + 3, Gr + Y.wm[l], Gr + Y.bm[l], s);
-		gemm<W, 2 * W, true>(rows_m, dzm, P + Y.wm[l], 2 * W + 3, 2 * W, W,
-		                     EStore{nullptr, N->dxm, nullptr, 2 * W, 2 * W, 0}, s);
-		k_scatter_msg<<<nb(rows_c, 4), 256, 0, s>>>(G, B, N->dxm, 2 * W, N->dh);
+		// messages: dZm = d[a] of the destination, masked by Zm > 0, summed per cell over
+		// outgoing (S_out) and incoming (S_in) messages; the first layer's weight and input
+		// gradients are cell-level GEMMs of S = [S_out, S_in]
+		const unsigned mb = std::min<unsigned>(nb(rows_c, 4), kMsgBackBlocks);
+		k_msg_back<<<mb, 256, 0, s>>>(G, B, mp, N->t2, KUPD, W, N->sgrad, N->epart);
+		k_reduce_edge<<<1, 256, 0, s>>>((int)mb, N->epart, Gr + Y.wm[l], Gr + Y.bm[l]);
+		wgrad<2 * W, W>(N, rows_c, LRows{N->sgrad, 2 * W, 2 * W}, LRows{hl, W, W}, W, 2 * W, Gr + Y.wm[l], nullptr, s,
+		                1);
+		const float *wst = N->wst + (size_t)l * 2 * W * W;
+		gemm<2 * W, W, true>(rows_c, LRows{N->sgrad, 2 * W, 2 * W}, wst, W, W, 2 * W, EAccum{N->dh, W}, s);
 		count_launches(4);
 	}
 	// encoder: h0 = relu(We x + be)

@@ -7,8 +7,12 @@ forward and backward kernels.
 Arithmetic is float64.  With ``bf16=True`` every GEMM operand is rounded to
 bfloat16 (round to nearest even) at the points where the GPU kernels stage
 them in shared memory, so the two differ only by the GPU's FP32 accumulation
-order and its FP32 intermediates.  With ``bf16=False`` the backward pass is
-checked against central finite differences of the loss.
+order and its FP32 intermediates.  The message MLP's first layer is applied
+per cell (W_s h and W_d h, gathered per message), which is the same sum of
+products; its backward pass goes through per-cell sums of the messages'
+gradients, which are rounded to bfloat16 as GEMM operands.  With
+``bf16=False`` the backward pass is checked against central finite
+differences of the loss.
 
 Parameter layout (flat float32 vector, as fv_mpnn_params):
     We [64][7], be [64], per layer l: Wm [64][131], bm [64], Wu [64][128], bu [64],
@@ -150,11 +154,19 @@ class Net:
                 dXu = r(dZu) @ r(P[f"wu{l}"])
                 da = dXu[:, W:]
                 dh = dh + dXu[:, :W]
+                # the message MLP's first layer is linear in h_src and h_dst, so its
+                # gradients go through per-cell sums of dZm over outgoing (S_out) and
+                # incoming (S_in) messages; these sums are the BF16-rounded operands
                 dZm = da[self.dst] * (S["zm"][l] > 0)
-                G[f"wm{l}"] += r(dZm).T @ r(S["xm"][l])
+                s_out = self._scatter(dZm, self.src)
+                s_in = self._scatter(dZm, self.dst)
+                h_l = S["hs"][l]
+                Wm = P[f"wm{l}"]
+                G[f"wm{l}"][:, :W] += r(s_out).T @ r(h_l)
+                G[f"wm{l}"][:, W:2 * W] += r(s_in).T @ r(h_l)
+                G[f"wm{l}"][:, 2 * W:] += dZm.T @ r(self.ea)
                 G[f"bm{l}"] += dZm.sum(0)
-                dXm = r(dZm) @ r(P[f"wm{l}"][:, :2 * W])
-                dh = dh + self._scatter(dXm[:, :W], self.src) + self._scatter(dXm[:, W:], self.dst)
+                dh = dh + r(s_out) @ r(Wm[:, :W]) + r(s_in) @ r(Wm[:, W:2 * W])
             dZ0 = dh * (S["Z0"] > 0)
             G["we"] += r(dZ0).T @ r(S["X"])
             G["be"] += dZ0.sum(0)
