@@ -323,18 +323,18 @@ def _laminar_conditions(fv, n, seed):
                            viscous=True) for k in range(n)]
 
 
-def _laminar_solvers(fv, m, plist, prec, starter=True):
+def _laminar_solvers(fv, m, plist, prec, starter=True, pc="ilu0"):
     """(discretisation, [starter solver,] main solver) for the conditions plist:
     first-order starter to a relative 1e-1 (at most 50 steps), then the
     second-order main solve to the absolute 1e-10."""
     main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), LAMINAR_BCS)
     S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
-                                      max_timesteps=600, pc="ilu0", nl_update=2, precision=prec)
+                                      max_timesteps=600, pc=pc, nl_update=2, precision=prec)
     if not starter:
         return main, [S2]
     start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS)
     S1 = fv.SteadyBackwardEulerSolver(start, cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0,
-                                      max_timesteps=50, pc="ilu0", nl_update=2, precision=prec)
+                                      max_timesteps=50, pc=pc, nl_update=2, precision=prec)
     return main, [S1, S2]
 
 
@@ -346,14 +346,15 @@ def run_batched(fv, torch, dev, B=64, seed=7):
     """Batched solves of B laminar conditions (M ~ U[0.3, 0.7], AoA ~ U[-4, 4] deg,
     Re ~ U[2000, 10000], Pr 0.72, adiabatic wall; Roe, least squares) on the
     reference's hybrid NACA 0012 mesh (13,156 cells), all members in the same
-    launches with FP32 Jacobians and ILU(0), against one member alone on the
-    FP32 path and on the plain FP64 path."""
+    launches with FP32 Jacobians and ILU(0) (and with block SGS), against one
+    member alone on the FP32 path and on the plain FP64 path."""
     import collections
     m, nlines = _laminar_mesh(fv)
     phs = _laminar_conditions(fv, B, seed)
     res = {"mesh_cells": m.nelem, "batch": B, "lines": nlines}
-    for tag, plist, prec in (("single_plain_fp64", phs[:1], 8), ("single", phs[:1], 4), ("batch", phs, 4)):
-        main, solvers = _laminar_solvers(fv, m, plist, prec)
+    for tag, plist, prec, pc in (("single_plain_fp64", phs[:1], 8, "ilu0"), ("single", phs[:1], 4, "ilu0"),
+                                 ("batch", phs, 4, "ilu0"), ("batch_sgs", phs, 4, "sgs")):
+        main, solvers = _laminar_solvers(fv, m, plist, prec, pc=pc)
         u = _freestream_field(torch, dev, main, m.nelem)
         t, stats = _timed_solve(torch, solvers, u, all_members=True)
         conv = sum(1 for st in stats if st["status"] == 0)

@@ -52,7 +52,7 @@ constexpr int GT = 128;      // GEMM CTA threads (4 warps x 16 rows)
 constexpr int GR = 64;       // GEMM rows per CTA
 constexpr int kWgradCtas = 608;  // weight-gradient CTAs (4 per SM of 152), each over many row chunks
 constexpr int kReduceSlices = 16;  // slices of the CTA partials in the gradient reduction
-constexpr int kMsgBackBlocks = 1216;  // blocks of the message-layer backward (8 per SM of 152)
+constexpr int kMsgBackBlocks = 608;  // blocks of the message-layer backward (4 per SM of 152)
 
 __device__ __forceinline__ unsigned pack_bf16(float lo, float hi)
 {
@@ -243,6 +243,19 @@ struct EUpdate {  // hn = h + relu(Z + bu), pre = Z + bu
 	}
 };
 
+struct ESplit {  // input gradient of the node update [d h | d a]: dh += the first W columns, da stored
+	float *dh, *da;   // da: row stride 2 W, columns W..2W-1 hold d a
+	__device__ void operator()(int r, int n, float z0, float z1) const
+	{
+		if (n < W) {
+			float2 *o = reinterpret_cast<float2 *>(dh + (size_t)r * W + n);
+			const float2 v = *o;
+			*o = make_float2(v.x + z0, v.y + z1);
+		} else {
+			*reinterpret_cast<float2 *>(da + (size_t)r * 2 * W + n) = make_float2(z0, z1);
+		}
+	}
+};
 struct EAccum {  // out += Z (row stride ldo)
 	float *out;
 	int ldo;
@@ -417,16 +430,32 @@ __global__ void k_reduce_final(int S, int nw, int nv, int kv, const float *tmp, 
 	}
 }
 
-/* a_i = sum of the messages relu(Zm) into cell i (fixed CSR order); 4 rows per block */
+__device__ __forceinline__ float4 relu4(float4 v)
+{
+	return make_float4(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f), fmaxf(v.z, 0.f), fmaxf(v.w, 0.f));
+}
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+/* v where z > 0, else 0 (per component) */
+__device__ __forceinline__ float4 mask4(float4 z, float4 v)
+{
+	return make_float4(z.x > 0.f ? v.x : 0.f, z.y > 0.f ? v.y : 0.f, z.z > 0.f ? v.z : 0.f, z.w > 0.f ? v.w : 0.f);
+}
+__device__ __forceinline__ float bfr(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+/* The message-level kernels use 16 threads per row, 4 columns each (float4),
+ * 256-thread blocks of 16 rows. */
+constexpr int MROWS = 16;
+
+/* a_i = sum of the messages relu(Zm) into cell i (fixed CSR order) */
 __global__ void k_aggregate(Graph G, int B, const float *zm, float *agg)
 {
-	const int r = blockIdx.x * 4 + (threadIdx.x >> 6), k = threadIdx.x & 63;
+	const int r = blockIdx.x * MROWS + (threadIdx.x >> 4), q4 = threadIdx.x & 15;
 	if (r >= B * G.nc) return;
 	const int b = r / G.nc, i = r - b * G.nc;
-	const float *mb = zm + (size_t)b * 2 * G.nf * W;
-	float s = 0.f;
-	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s += fmaxf(mb[(size_t)G.in_idx[q] * W + k], 0.f);
-	agg[(size_t)r * W + k] = s;
+	const float4 *mb = reinterpret_cast<const float4 *>(zm + (size_t)b * 2 * G.nf * W);
+	float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+	for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) s = add4(s, relu4(mb[(size_t)G.in_idx[q] * (W / 4) + q4]));
+	reinterpret_cast<float4 *>(agg)[(size_t)r * (W / 4) + q4] = s;
 }
 
 /* Wst [128][64]: rows 0..63 the message weights' h_src block W_s, rows
@@ -441,22 +470,33 @@ __global__ void k_stack_w(const float *wm, float *wst)
 
 /* Zm = W_s h_src + W_d h_dst + W_e e + bm from the per-cell projections
  * pc = [W_s h, W_d h] (row stride 2 W); the edge term with BF16-rounded W_e and
- * e, as the GEMM operands.  4 messages x 64 columns per block. */
+ * e, as the GEMM operands. */
 __global__ void k_msg_fwd(Graph G, int B, const float *pc, const float *wm, const float *bm, float *zm)
 {
-	const int r = blockIdx.x * 4 + (threadIdx.x >> 6), n = threadIdx.x & 63;
+	__shared__ float swe[W][3];
+	for (int e = threadIdx.x; e < 3 * W; e += blockDim.x) {
+		const int n = e / 3, c = e - 3 * n;
+		swe[n][c] = bfr(wm[(size_t)n * (2 * W + 3) + 2 * W + c]);
+	}
+	__syncthreads();
+	const int r = blockIdx.x * MROWS + (threadIdx.x >> 4), q4 = threadIdx.x & 15;
 	const int per = 2 * G.nf;
 	if (r >= B * per) return;
 	const int b = r / per;
 	int src, dst;
 	float4 e;
 	msg_ends(G, r - b * per, src, dst, e);
-	const size_t cs = (size_t)b * G.nc + src, cd = (size_t)b * G.nc + dst;
-	const float *we = wm + (size_t)n * (2 * W + 3) + 2 * W;
-	const float bfe = __bfloat162float(__float2bfloat16_rn(e.x)) * __bfloat162float(__float2bfloat16_rn(we[0])) +
-	                  __bfloat162float(__float2bfloat16_rn(e.y)) * __bfloat162float(__float2bfloat16_rn(we[1])) +
-	                  __bfloat162float(__float2bfloat16_rn(e.z)) * __bfloat162float(__float2bfloat16_rn(we[2]));
-	zm[(size_t)r * W + n] = pc[cs * 2 * W + n] + pc[cd * 2 * W + W + n] + bfe + bm[n];
+	const float ex = bfr(e.x), ey = bfr(e.y), ez = bfr(e.z);
+	const float4 ps = reinterpret_cast<const float4 *>(pc + ((size_t)b * G.nc + src) * 2 * W)[q4];
+	const float4 pd = reinterpret_cast<const float4 *>(pc + ((size_t)b * G.nc + dst) * 2 * W + W)[q4];
+	const float4 bb = reinterpret_cast<const float4 *>(bm)[q4];
+	float z[4];
+	const float a0[4] = {ps.x, ps.y, ps.z, ps.w}, a1[4] = {pd.x, pd.y, pd.z, pd.w}, a2[4] = {bb.x, bb.y, bb.z, bb.w};
+	for (int j = 0; j < 4; j++) {
+		const int n = 4 * q4 + j;
+		z[j] = a0[j] + a1[j] + (ex * swe[n][0] + ey * swe[n][1] + ez * swe[n][2]) + a2[j];
+	}
+	reinterpret_cast<float4 *>(zm)[(size_t)r * (W / 4) + q4] = make_float4(z[0], z[1], z[2], z[3]);
 }
 
 /* Message-layer backward from da (the aggregate's gradient, columns off.. of
@@ -465,70 +505,75 @@ __global__ void k_msg_fwd(Graph G, int B, const float *pc, const float *wm, cons
  * edge-weight and bias gradients sum_m dZm e_m, sum_m dZm accumulated over
  * each cell's incoming messages (every message once), per thread in fixed
  * order over the cells it visits, then per block in fixed order into
- * epart[block][64][4].  4 cells x 64 columns per block, grid-stride over cells. */
+ * epart[block][64][4].  Grid-stride over cells. */
 __global__ void k_msg_back(Graph G, int B, const float *zm, const float *dagg, int lda, int off, float *S,
                            float *epart)
 {
-	const int n = threadIdx.x & 63, slot = threadIdx.x >> 6;
+	const int q4 = threadIdx.x & 15, slot = threadIdx.x >> 4;
 	const int rows = B * G.nc;
 	const size_t per = 2 * (size_t)G.nf;
-	float ae[4] = {0.f, 0.f, 0.f, 0.f};
-	for (int r = blockIdx.x * 4 + slot; r < rows; r += gridDim.x * 4) {
+	float ae[4][4] = {};  // [column j][e0, e1, e2, bias]
+	for (int r = blockIdx.x * MROWS + slot; r < rows; r += gridDim.x * MROWS) {
 		const int b = r / G.nc, i = r - b * G.nc;
-		const float *zb = zm + (size_t)b * per * W;
-		const float di = dagg[(size_t)r * lda + off + n];
-		float sin_ = 0.f, sout = 0.f;
+		const float4 *zb = reinterpret_cast<const float4 *>(zm + (size_t)b * per * W);
+		const float4 di = reinterpret_cast<const float4 *>(dagg + (size_t)r * lda + off)[q4];
+		float4 sin_ = make_float4(0.f, 0.f, 0.f, 0.f), sout = sin_;
 		for (int q = G.in_ptr[i]; q < G.in_ptr[i + 1]; q++) {
 			const int m = G.in_idx[q];
-			const float dz = zb[(size_t)m * W + n] > 0.f ? di : 0.f;
-			sin_ += dz;
+			const float4 dz = mask4(zb[(size_t)m * (W / 4) + q4], di);
+			sin_ = add4(sin_, dz);
 			int s0, d0;
 			float4 e;
 			msg_ends(G, m, s0, d0, e);
-			ae[0] += dz * __bfloat162float(__float2bfloat16_rn(e.x));
-			ae[1] += dz * __bfloat162float(__float2bfloat16_rn(e.y));
-			ae[2] += dz * __bfloat162float(__float2bfloat16_rn(e.z));
-			ae[3] += dz;
+			const float ee[3] = {bfr(e.x), bfr(e.y), bfr(e.z)};
+			const float dzs[4] = {dz.x, dz.y, dz.z, dz.w};
+			for (int j = 0; j < 4; j++) {
+				for (int c = 0; c < 3; c++) ae[j][c] += dzs[j] * ee[c];
+				ae[j][3] += dzs[j];
+			}
 		}
 		for (int q = G.out_ptr[i]; q < G.out_ptr[i + 1]; q++) {
 			const int m = G.out_idx[q];
 			int s0, d0;
 			float4 e;
 			msg_ends(G, m, s0, d0, e);
-			const float dd = dagg[((size_t)b * G.nc + d0) * lda + off + n];
-			sout += zb[(size_t)m * W + n] > 0.f ? dd : 0.f;
+			const float4 dd = reinterpret_cast<const float4 *>(dagg + ((size_t)b * G.nc + d0) * lda + off)[q4];
+			sout = add4(sout, mask4(zb[(size_t)m * (W / 4) + q4], dd));
 		}
-		S[(size_t)r * 2 * W + n] = sout;
-		S[(size_t)r * 2 * W + W + n] = sin_;
+		reinterpret_cast<float4 *>(S + (size_t)r * 2 * W)[q4] = sout;
+		reinterpret_cast<float4 *>(S + (size_t)r * 2 * W + W)[q4] = sin_;
 	}
-	__shared__ float sh[4][64][4];
-	for (int k = 0; k < 4; k++) sh[slot][n][k] = ae[k];
+	__shared__ float sh[MROWS][W][4];
+	for (int j = 0; j < 4; j++)
+		for (int c = 0; c < 4; c++) sh[slot][4 * q4 + j][c] = ae[j][c];
 	__syncthreads();
-	if (threadIdx.x < 64)
-		for (int k = 0; k < 4; k++)
-			epart[((size_t)blockIdx.x * 64 + n) * 4 + k] = sh[0][n][k] + sh[1][n][k] + sh[2][n][k] + sh[3][n][k];
+	{
+		const int n = threadIdx.x >> 2, c = threadIdx.x & 3;  // 256 threads: 64 columns x 4
+		float t = 0.f;
+		for (int k = 0; k < MROWS; k++) t += sh[k][n][c];
+		epart[((size_t)blockIdx.x * W + n) * 4 + c] = t;
+	}
 }
 
-/* edge-weight columns and bias of a message layer's gradient: sum of the
- * block partials in fixed order */
+/* edge-weight columns and bias of a message layer's gradient: one block per
+ * (column n, component c): the block partials summed in a fixed order (strided
+ * per thread, then a shared-memory tree) */
 __global__ void k_reduce_edge(int nblk, const float *epart, float *gwm, float *gbm)
 {
-	const int e = blockIdx.x * blockDim.x + threadIdx.x;  // (n, k), k < 4
-	if (e >= 64 * 4) return;
-	const int n = e >> 2, k = e & 3;
-	float s = 0.f;
-	for (int c = 0; c < nblk; c++) s += epart[((size_t)c * 64 + n) * 4 + k];
-	if (k < 3) gwm[(size_t)n * (2 * W + 3) + 2 * W + k] += s;
-	else gbm[n] += s;
-}
-
-/* dh[r][k] += dX[r][k] for k < W (dX row stride ld) */
-__global__ void k_add_cols(size_t rows, const float *src, int lds, float *dst)
-{
-	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-	if (e >= rows * W) return;
-	const size_t r = e / W, k = e - r * W;
-	dst[e] += src[r * lds + k];
+	__shared__ float sh[128];
+	const int n = blockIdx.x >> 2, c = blockIdx.x & 3;
+	float t = 0.f;
+	for (int k = threadIdx.x; k < nblk; k += 128) t += epart[((size_t)k * W + n) * 4 + c];
+	sh[threadIdx.x] = t;
+	__syncthreads();
+	for (int o = 64; o > 0; o >>= 1) {
+		if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		if (c < 3) gwm[(size_t)n * (2 * W + 3) + 2 * W + c] += sh[0];
+		else gbm[n] += sh[0];
+	}
 }
 
 /* u = uinf + scale * y (double) */
@@ -715,9 +760,9 @@ cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
 		k_stack_w<<<nb(2 * W * W, 256), 256, 0, s>>>(P + Y.wm[l], wst);
 		gemm<W, 2 * W, false>(rows_c, LRows{hl, W, W}, wst, W, 2 * W, W, EStore{nullptr, N->pc, nullptr, 2 * W, 2 * W, 0},
 		                      s);
-		k_msg_fwd<<<nb(rows_m, 4), 256, 0, s>>>(G, B, N->pc, P + Y.wm[l], P + Y.bm[l], mp);
+		k_msg_fwd<<<nb(rows_m, MROWS), 256, 0, s>>>(G, B, N->pc, P + Y.wm[l], P + Y.bm[l], mp);
 		float *al = N->agg + l * rows_c * W;
-		k_aggregate<<<nb(rows_c, 4), 256, 0, s>>>(G, B, mp, al);
+		k_aggregate<<<nb(rows_c, MROWS), 256, 0, s>>>(G, B, mp, al);
 		gemm<KUPD, W, false>(rows_c, LUpd{hl, al}, P + Y.wu[l], KUPD, W, KUPD,
 		                     EUpdate{P + Y.bu[l], hl, N->h + (l + 1) * rows_c * W, N->upre + l * rows_c * W}, s);
 	}
@@ -762,16 +807,15 @@ cudaError_t backward(fv_mpnn *N, int B, cudaStream_t s)
 		const float *up = N->upre + l * rows_c * W, *mp = N->mpre + l * rows_m * W;
 		// update: hn = h + relu(Zu), Zu = Wu [h, a] + bu;  dZu = dh (Zu > 0)
 		wgrad<KUPD, W>(N, rows_c, LUpd{hl, al}, LRelu{N->dh, up}, W, KUPD, Gr + Y.wu[l], Gr + Y.bu[l], s);
-		gemm<W, KUPD, true>(rows_c, LRelu{N->dh, up}, P + Y.wu[l], KUPD, KUPD, W,
-		                    EStore{nullptr, N->t2, nullptr, KUPD, KUPD, 0}, s);
-		// residual path plus the update's d[h] columns
-		k_add_cols<<<nb(rows_c * W, 256), 256, 0, s>>>(rows_c, N->t2, KUPD, N->dh);
+		// dh (residual path) += the update's d[h] columns; d[a] into t2 (columns W..2W-1).
+		// Each CTA reads and then updates only its own rows of dh.
+		gemm<W, KUPD, true>(rows_c, LRelu{N->dh, up}, P + Y.wu[l], KUPD, KUPD, W, ESplit{N->dh, N->t2}, s);
 		// messages: dZm = d[a] of the destination, masked by Zm > 0, summed per cell over
 		// outgoing (S_out) and incoming (S_in) messages; the first layer's weight and input
 		// gradients are cell-level GEMMs of S = [S_out, S_in]
-		const unsigned mb = std::min<unsigned>(nb(rows_c, 4), kMsgBackBlocks);
+		const unsigned mb = std::min<unsigned>(nb(rows_c, MROWS), kMsgBackBlocks);
 		k_msg_back<<<mb, 256, 0, s>>>(G, B, mp, N->t2, KUPD, W, N->sgrad, N->epart);
-		k_reduce_edge<<<1, 256, 0, s>>>((int)mb, N->epart, Gr + Y.wm[l], Gr + Y.bm[l]);
+		k_reduce_edge<<<4 * W, 128, 0, s>>>((int)mb, N->epart, Gr + Y.wm[l], Gr + Y.bm[l]);
 		wgrad<2 * W, W>(N, rows_c, LRows{N->sgrad, 2 * W, 2 * W}, LRows{hl, W, W}, W, 2 * W, Gr + Y.wm[l], nullptr, s,
 		                1);
 		const float *wst = N->wst + (size_t)l * 2 * W * W;
