@@ -22,7 +22,7 @@ RECONSTRUCTION = {"NONE": 0, "VANALBADA": 1, "BARTHJESPERSEN": 2, "VENKATAKRISHN
 BC = {"slipwall": 0, "farfield": 1, "inflowoutflow": 2, "subsonic_inflow": 3, "extrapolation": 4,
       "periodic": 5, "isothermalwall": 6, "adiabaticwall": 7}
 PC = {"none": 0, "jacobi": 1, "sgs": 2, "ilu0": 3}
-MESH_CHANNEL_BUMP, MESH_NACA_OGRID = 1, 2
+MESH_CHANNEL_BUMP, MESH_NACA_OGRID, MESH_NACA_HYBRID = 1, 2, 3
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_dbl_p = ctypes.POINTER(ctypes.c_double)

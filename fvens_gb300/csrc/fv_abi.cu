@@ -165,6 +165,12 @@ fv_status fv_mesh_generate(int kind, const double *p, int np, int reorder, fv_me
 		r = gen_channel_bump((int)p[0], (int)p[1], p[2], (uint64_t)p[3]);
 	} else if (kind == FV_MESH_NACA_OGRID && np >= 8) {
 		r = gen_naca_ogrid((int)p[0], (int)p[1], p[2], (int)p[3], p[4], p[5], (int)p[6], (uint64_t)p[7]);
+	} else if (kind == FV_MESH_NACA_HYBRID && np >= 6) {
+		if (p[0] < 8 || p[1] < 0 || p[2] <= 0 || p[3] < 1 || p[4] <= 1 || p[5] < 0 || p[5] > 1) {
+			set_error("invalid hybrid NACA mesh parameters");
+			return FV_ERR_INVALID;
+		}
+		r = gen_naca_hybrid((int)p[0], (int)p[1], p[2], p[3], p[4], p[5]);
 	} else {
 		set_error("unknown mesh kind or too few parameters");
 		return FV_ERR_INVALID;

@@ -506,6 +506,154 @@ RawMesh gen_naca_ogrid(int nc, int nr, double rfar, int nbl, double h0, double g
 	return r;
 }
 
+/* Hybrid NACA 0012 mesh with near-isotropic outer triangles.  Surface: nc
+ * points, x = (1 - beta) cosine spacing + beta uniform spacing (beta bounds
+ * the clustering at the leading and trailing edges).  Boundary layer: nbl quad
+ * rings extruded with heights h0 g^k along the surface normals, lightly
+ * smoothed; towards the closed trailing edge (x from 0.7 to 0.95) they blend
+ * into heavily smoothed normals, which spread the trailing-edge fan over many
+ * nodes.  Outer region: each ring is the previous one offset along its
+ * normals by sqrt(3)/2 times its mean edge length (near-equilateral
+ * triangles, geometric growth), then resampled by arc length at parameters
+ * that drift by 3 % per ring from the boundary layer's distribution towards
+ * uniform spacing; rings are added until every node is at least rfar from
+ * mid-chord.  Quads between outer rings are split along the shorter diagonal. */
+RawMesh gen_naca_hybrid(int nc, int nbl, double h0, double gbl, double rfar, double beta)
+{
+	const double PI = 3.14159265358979323846;
+	RawMesh r;
+	std::vector<double> px(nc), py(nc);
+	for (int i = 0; i < nc; i++) {
+		const double t = (double)i / nc;
+		const double xc = 0.5 * (1.0 + std::cos(2.0 * PI * t));
+		const double xu = t <= 0.5 ? 1.0 - 2.0 * t : 2.0 * t - 1.0;
+		const double x = (1.0 - beta) * xc + beta * xu;
+		const double yt = naca0012_half(x);
+		px[i] = x;
+		py[i] = (i == 0 || 2 * i == nc) ? 0.0 : (2 * i < nc ? yt : -yt);
+	}
+	// outward unit normals of a closed counter-clockwise ring, then `passes`
+	// rounds of [1/4 1/2 1/4] smoothing along the ring
+	auto normals = [&](const std::vector<double> &x, const std::vector<double> &y, std::vector<double> &nx,
+	                   std::vector<double> &ny, int passes) {
+		nx.assign(nc, 0.0);
+		ny.assign(nc, 0.0);
+		for (int i = 0; i < nc; i++) {
+			const int ip = (i + 1) % nc, im = (i + nc - 1) % nc;
+			const double tx = x[ip] - x[im], ty = y[ip] - y[im];
+			const double l = std::sqrt(tx * tx + ty * ty);
+			nx[i] = ty / l;
+			ny[i] = -tx / l;
+		}
+		std::vector<double> ax(nc), ay(nc);
+		for (int it = 0; it < passes; it++) {
+			for (int i = 0; i < nc; i++) {
+				const int ip = (i + 1) % nc, im = (i + nc - 1) % nc;
+				ax[i] = 0.5 * nx[i] + 0.25 * (nx[ip] + nx[im]);
+				ay[i] = 0.5 * ny[i] + 0.25 * (ny[ip] + ny[im]);
+				const double l = std::sqrt(ax[i] * ax[i] + ay[i] * ay[i]);
+				ax[i] /= l;
+				ay[i] /= l;
+			}
+			nx.swap(ax);
+			ny.swap(ay);
+		}
+	};
+	std::vector<std::vector<double>> rx, ry;  // rings, 0 = the surface
+	rx.push_back(px);
+	ry.push_back(py);
+	std::vector<double> nx, ny, sx, sy;
+	normals(px, py, nx, ny, 4);
+	normals(px, py, sx, sy, 200);
+	for (int i = 0; i < nc; i++) {
+		const double w = std::min(1.0, std::max(0.0, (px[i] - 0.7) / 0.25));
+		const double ax = w * sx[i] + (1 - w) * nx[i], ay = w * sy[i] + (1 - w) * ny[i];
+		const double l = std::sqrt(ax * ax + ay * ay);
+		nx[i] = ax / l;
+		ny[i] = ay / l;
+	}
+	double d = 0.0;
+	for (int k = 1; k <= nbl; k++) {
+		d += h0 * std::pow(gbl, k - 1);
+		std::vector<double> x(nc), y(nc);
+		for (int i = 0; i < nc; i++) { x[i] = px[i] + d * nx[i]; y[i] = py[i] + d * ny[i]; }
+		rx.push_back(x);
+		ry.push_back(y);
+	}
+	// arc-length parameter (fraction of the perimeter from node 0) of a closed ring's nodes
+	auto arclen = [&](const std::vector<double> &x, const std::vector<double> &y, std::vector<double> &cs) {
+		cs.assign(nc + 1, 0.0);
+		for (int i = 0; i < nc; i++) cs[i + 1] = cs[i] + std::hypot(x[(i + 1) % nc] - x[i], y[(i + 1) % nc] - y[i]);
+		return cs[nc];
+	};
+	std::vector<double> cs, s(nc);
+	{
+		const double P = arclen(rx.back(), ry.back(), cs);
+		for (int i = 0; i < nc; i++) s[i] = cs[i] / P;
+	}
+	const int max_rings = 100000;
+	for (int it = 0; it < max_rings; it++) {
+		const std::vector<double> &x = rx.back(), &y = ry.back();
+		double rmin = 1e300;
+		for (int i = 0; i < nc; i++) rmin = std::min(rmin, std::hypot(x[i] - 0.5, y[i]));
+		if (rmin >= rfar) break;
+		const double h = arclen(x, y, cs) / nc;
+		normals(x, y, nx, ny, 2);
+		std::vector<double> ox(nc), oy(nc), X(nc), Y(nc);
+		for (int i = 0; i < nc; i++) {
+			ox[i] = x[i] + 0.8660254037844386 * h * nx[i];
+			oy[i] = y[i] + 0.8660254037844386 * h * ny[i];
+		}
+		const double P = arclen(ox, oy, cs);
+		int seg = 0;
+		for (int i = 0; i < nc; i++) {
+			s[i] = 0.97 * s[i] + 0.03 * ((double)i / nc);
+			const double t = s[i] * P;
+			while (seg < nc - 1 && cs[seg + 1] < t) seg++;
+			const double f = cs[seg + 1] > cs[seg] ? (t - cs[seg]) / (cs[seg + 1] - cs[seg]) : 0.0;
+			const int j = (seg + 1) % nc;
+			X[i] = ox[seg] + f * (ox[j] - ox[seg]);
+			Y[i] = oy[seg] + f * (oy[j] - oy[seg]);
+		}
+		rx.push_back(X);
+		ry.push_back(Y);
+	}
+	const int nr = (int)rx.size() - 1;
+	r.npoin = nc * (nr + 1);
+	r.coords.resize(2 * (size_t)r.npoin);
+	for (int k = 0; k <= nr; k++)
+		for (int i = 0; i < nc; i++) {
+			r.coords[2 * ((size_t)k * nc + i)] = rx[k][i];
+			r.coords[2 * ((size_t)k * nc + i) + 1] = ry[k][i];
+		}
+	auto node = [&](int i, int k) { return k * nc + (i % nc); };
+	auto dist2 = [&](int a, int b) {
+		const double dx = r.coords[2 * (size_t)a] - r.coords[2 * (size_t)b];
+		const double dy = r.coords[2 * (size_t)a + 1] - r.coords[2 * (size_t)b + 1];
+		return dx * dx + dy * dy;
+	};
+	for (int k = 0; k < nr; k++)
+		for (int i = 0; i < nc; i++) {
+			// (i,k) -> (i,k+1) -> (i+1,k+1) -> (i+1,k) is counter-clockwise
+			const int a = node(i, k), b = node(i, k + 1), c = node(i + 1, k + 1), e = node(i + 1, k);
+			if (k < nbl) {
+				r.nnode.push_back(4);
+				r.inpoel.insert(r.inpoel.end(), {a, b, c, e});
+			} else if (dist2(a, c) <= dist2(b, e)) {
+				r.nnode.push_back(3); r.inpoel.insert(r.inpoel.end(), {a, b, c, -1});
+				r.nnode.push_back(3); r.inpoel.insert(r.inpoel.end(), {a, c, e, -1});
+			} else {
+				r.nnode.push_back(3); r.inpoel.insert(r.inpoel.end(), {a, b, e, -1});
+				r.nnode.push_back(3); r.inpoel.insert(r.inpoel.end(), {b, c, e, -1});
+			}
+		}
+	r.nelem = (int)r.nnode.size();
+	for (int i = 0; i < nc; i++) { r.bface.insert(r.bface.end(), {node(i, 0), node(i + 1, 0)}); r.btag.push_back(2); }
+	for (int i = 0; i < nc; i++) { r.bface.insert(r.bface.end(), {node(i, nr), node(i + 1, nr)}); r.btag.push_back(4); }
+	r.nbface = (int)r.btag.size();
+	return r;
+}
+
 namespace {
 /* next "KEY=value" header of an SU2 file: the value as an integer (tags and
  * counts are numeric in the meshes this reader supports) */

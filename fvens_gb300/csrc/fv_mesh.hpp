@@ -116,6 +116,7 @@ RawMesh gen_channel_bump(int nx, int ny, double split_frac, uint64_t seed);
  * last ring reaches the far field.  Rings with index >= tri_from are split into
  * triangles along seeded diagonals.  Markers: 2 airfoil wall, 4 far field. */
 RawMesh gen_naca_ogrid(int nc, int nr, double rfar, int nbl, double h0, double gbl, int tri_from, uint64_t seed);
+RawMesh gen_naca_hybrid(int nc, int nbl, double h0, double gbl, double rfar, double beta);
 
 /* Gmsh 2.2 ASCII reader: line elements (type 1) are boundary faces with
  * their first tag as marker; triangles (2) and quads (3) are cells. */

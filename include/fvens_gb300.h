@@ -79,6 +79,8 @@ typedef int fv_status;
 /* synthetic meshes for fv_mesh_generate */
 #define FV_MESH_CHANNEL_BUMP 1  /* params: nx, ny, split_fraction, seed */
 #define FV_MESH_NACA_OGRID 2    /* params: nc, nr, rfar, nbl, h0, growth, tri_from_ring, seed */
+#define FV_MESH_NACA_HYBRID 3   /* params: nc, nbl, h0, growth, rfar, beta: quad boundary layer, near-isotropic
+                                   outer triangles marched out to rfar (beta in [0,1] bounds surface clustering) */
 
 typedef struct fv_mesh fv_mesh;
 typedef struct fv_disc fv_disc;

@@ -254,3 +254,27 @@ def test_find_lines_on_boundary_layer_mesh():
     assert cases.channel(24, 8).find_lines(10.0)[0] == 0
     # threshold <= 0 removes them
     assert m.find_lines(0.0)[0] == 0
+
+
+def test_hybrid_naca_generator_quality():
+    """FV_MESH_NACA_HYBRID at the 400k-cell laminar configuration: 48 quad
+    boundary-layer rings from 1e-4 chords (growth 1.12) and near-isotropic
+    outer triangles to 20 chords -- every cell positive, no triangle angle
+    under 5 degrees, far-field nodes at >= 20 chords."""
+    m = fv.UMesh.generate(fv.MESH_NACA_HYBRID, [512, 48, 1e-4, 1.12, 20.0, 0.5], reorder=0)
+    ex, g = m.export(), m.geometry()
+    assert m.nelem == 381952 and int((ex["nnode"] == 4).sum()) == 512 * 48
+    assert g["area"].min() > 0
+    X, P = ex["coords"], ex["inpoel"]
+    tri = P[ex["nnode"] == 3][:, :3]
+    pts = X[tri]
+    ang = []
+    for j in range(3):
+        v1, v2 = pts[:, (j + 1) % 3] - pts[:, j], pts[:, (j - 1) % 3] - pts[:, j]
+        c = (v1 * v2).sum(1) / np.linalg.norm(v1, axis=1) / np.linalg.norm(v2, axis=1)
+        ang.append(np.degrees(np.arccos(np.clip(c, -1, 1))))
+    assert np.min(ang) > 5.0
+    far = ex["bface"][ex["btag"] == 4].ravel()
+    assert np.hypot(X[far, 0] - 0.5, X[far, 1]).min() >= 20.0
+    with pytest.raises(fv.FvensError):
+        fv.UMesh.generate(fv.MESH_NACA_HYBRID, [512, 48, 1e-4, 1.12, 20.0, 1.5])
