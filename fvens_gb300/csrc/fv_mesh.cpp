@@ -510,9 +510,8 @@ RawMesh gen_naca_ogrid(int nc, int nr, double rfar, int nbl, double h0, double g
  * points, x = (1 - beta) cosine spacing + beta uniform spacing (beta bounds
  * the clustering at the leading and trailing edges).  Boundary layer: nbl quad
  * rings extruded with heights h0 g^k along the surface normals, lightly
- * smoothed; towards the closed trailing edge (x from 0.7 to 0.95) they blend
- * into heavily smoothed normals, which spread the trailing-edge fan over many
- * nodes.  Outer region: each ring is the previous one offset along its
+ * smoothed (the cells stay close to orthogonal up to the trailing-edge fan).
+ * Outer region: each ring is the previous one offset along its
  * normals by sqrt(3)/2 times its mean edge length (near-equilateral
  * triangles, geometric growth), then resampled by arc length at parameters
  * that drift by 3 % per ring from the boundary layer's distribution towards
@@ -562,16 +561,8 @@ RawMesh gen_naca_hybrid(int nc, int nbl, double h0, double gbl, double rfar, dou
 	std::vector<std::vector<double>> rx, ry;  // rings, 0 = the surface
 	rx.push_back(px);
 	ry.push_back(py);
-	std::vector<double> nx, ny, sx, sy;
+	std::vector<double> nx, ny;
 	normals(px, py, nx, ny, 4);
-	normals(px, py, sx, sy, 200);
-	for (int i = 0; i < nc; i++) {
-		const double w = std::min(1.0, std::max(0.0, (px[i] - 0.7) / 0.25));
-		const double ax = w * sx[i] + (1 - w) * nx[i], ay = w * sy[i] + (1 - w) * ny[i];
-		const double l = std::sqrt(ax * ax + ay * ay);
-		nx[i] = ax / l;
-		ny[i] = ay / l;
-	}
 	double d = 0.0;
 	for (int k = 1; k <= nbl; k++) {
 		d += h0 * std::pow(gbl, k - 1);
