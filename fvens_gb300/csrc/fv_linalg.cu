@@ -565,13 +565,12 @@ __global__ void __launch_bounds__(PT) k_ilu_parts(int nelem, int part0, int cap,
 		}
 	}
 	__syncthreads();
-	if (threadIdx.x < 32) {
-		const int lane = threadIdx.x;
+	{
 		const int l0 = lev_ptr[part], l1 = lev_ptr[part + 1];
-		const int g = lane >> 2, row = lane & 3;
+		const int g = threadIdx.x >> 2, row = threadIdx.x & 3;
 		for (int l = l0; l < l1; l++) {
 			const int ls = lev_pos[l] - p0, le = (l + 1 < l1 ? lev_pos[l + 1] : p1) - p0;
-			for (int c0 = ls; c0 < le; c0 += 8) {
+			for (int c0 = ls; c0 < le; c0 += PT / 4) {
 				const int c = c0 + g;
 				const bool on = c < le;
 				if (on) {
@@ -622,6 +621,7 @@ __global__ void __launch_bounds__(PT) k_ilu_parts(int nelem, int part0, int cap,
 				}
 				__syncwarp();
 			}
+			__syncthreads();  // the level's rows and inverted diagonals are read by later levels
 		}
 	}
 	__syncthreads();
