@@ -121,6 +121,8 @@ cudaError_t gradients_launch(fv_disc_impl *D, const double *u, double *grad, int
 /* the residual's passes before the face kernel (primitive/ghost states,
  * gradients, limiter values, WENO blend) into the handle's scratch */
 cudaError_t gradient_pass_launch(fv_disc_impl *D, const double *u, cudaStream_t s);
+cudaError_t residual_mf_launch(fv_disc_impl *D, const double *up, const double *x, const double *r, const double *dtm,
+                               const double *pm, double *y, cudaStream_t s);
 /* times the residual kernels at 64 / 128 / 256 threads per block at state u
  * and keeps the fastest per kernel in D->bs; chosen[4] (may be NULL) receives them */
 cudaError_t residual_autotune(fv_disc_impl *D, const double *u, cudaStream_t s, int *chosen);

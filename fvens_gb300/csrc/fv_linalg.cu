@@ -833,18 +833,29 @@ __global__ void k_givens(Krylov K, int nblk, int maxit)
 	if (!K.active[b]) return;
 	const int j = *K.jcur;
 	const double hn = sqrt(block_sum(K.part + ((size_t)b * (K.restart + 2) + K.restart + 1) * nblk, nblk));
-	if (threadIdx.x != 0) return;
 	const int m = K.restart;
 	double *H = K.H + (size_t)b * (m + 1) * m;
 	double *cs = K.cs + (size_t)b * (m + 1), *sn = K.sn + (size_t)b * (m + 1), *g = K.g + (size_t)b * (m + 1);
 	double *sc = K.scal + 8 * b;
-	H[(size_t)(j + 1) * m + j] = hn;
-	for (int i = 0; i < j; i++) {
-		const double a = H[(size_t)i * m + j], c = H[(size_t)(i + 1) * m + j];
-		H[(size_t)i * m + j] = cs[i] * a + sn[i] * c;
-		H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+	// column j and the previous rotations staged in shared memory by the warp, so the
+	// serial rotation chain below waits on shared memory, not on global loads
+	extern __shared__ double gsh[];  // [3][m + 1]: column j, cs, sn
+	double *hc = gsh, *cc = gsh + (m + 1), *ss = gsh + 2 * (m + 1);
+	for (int i = threadIdx.x; i <= j; i += 32) {
+		hc[i] = H[(size_t)i * m + j];
+		cc[i] = cs[i];
+		ss[i] = sn[i];
 	}
-	const double a = H[(size_t)j * m + j], c = H[(size_t)(j + 1) * m + j];
+	__syncwarp();
+	if (threadIdx.x != 0) return;
+	hc[j + 1] = hn;
+	for (int i = 0; i < j; i++) {
+		const double a = hc[i], c = hc[i + 1];
+		hc[i] = cc[i] * a + ss[i] * c;
+		hc[i + 1] = -ss[i] * a + cc[i] * c;
+	}
+	for (int i = 0; i < j; i++) H[(size_t)i * m + j] = hc[i];
+	const double a = hc[j], c = hc[j + 1];
 	const double den = sqrt(a * a + c * c);
 	cs[j] = a / den;
 	sn[j] = c / den;
@@ -1137,7 +1148,7 @@ static cudaError_t arnoldi_step(Krylov &K, LinOp &op, const Precond &P, int maxi
 	k_dot_partial<<<dim3(nb, B, maxit), RBS, 0, s>>>(n, nb, K.V, n, vstep, K.w, n, K.part, 0, m + 2, K.active, K.jcur);
 	k_reduce_h<<<dim3(B, maxit), 32, 0, s>>>(K, nb);
 	k_cgs_update<<<dim3(nb, B), RBS, 0, s>>>(K, nb);
-	k_givens<<<B, 32, 0, s>>>(K, nb, maxit);
+	k_givens<<<B, 32, sizeof(double) * 3 * (m + 1), s>>>(K, nb, maxit);
 	k_next_basis<<<dim3((unsigned)((n + 255) / 256), B), 256, 0, s>>>(K);
 	k_loop_ctrl<<<1, 32, 0, s>>>(K, maxit, h, set_cond);
 	*nk += 6;

@@ -68,6 +68,36 @@ __global__ void __launch_bounds__(kMaxBS) k_gather(DiscDev D, ResidualWork w, do
 	gather_body(D, b, i, w, r, dt);
 }
 
+/* The matrix-free product's last step fused into the gather: with a the
+ * gathered -R(u + pm x) of cell i, y_i = dtm_i x_i + (r_i - a) / pm, r = -R(u)
+ * (MatrixFreeSpatialJacobian::apply, alinalg.cpp:200-230) */
+__global__ void __launch_bounds__(kMaxBS) k_gather_mf(DiscDev D, ResidualWork w, const double *__restrict__ x,
+                                                      const double *__restrict__ r, const double *__restrict__ dtm,
+                                                      const double *__restrict__ pm, double *__restrict__ y)
+{
+	const int b = blockIdx.y;
+	if (skip_member(D, b)) return;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= D.nelem) return;
+	const int4 cf = D.cface[i];
+	const int fl[4] = {cf.x, cf.y, cf.z, cf.w};
+	double a[4] = {0, 0, 0, 0};
+	const d4 *ff = w.fflux + (size_t)b * D.naface;
+	for (int j = 0; j < 4; j++) {
+		if (fl[j] < 0) continue;
+		const int f = fl[j] >> 1, side = fl[j] & 1;
+		const d4 F = ff[f];
+		if (side) { a[0] += F.x; a[1] += F.y; a[2] += F.z; a[3] += F.w; }
+		else { a[0] -= F.x; a[1] -= F.y; a[2] -= F.z; a[3] -= F.w; }
+	}
+	const size_t c = (size_t)b * D.nelem + i;
+	const d4 xv = reinterpret_cast<const d4 *>(x)[c], rv = reinterpret_cast<const d4 *>(r)[c];
+	const double dv = dtm[c], p = pm[b];
+	// the gathered value is 0 + a, as in the unfused gather into a zeroed vector
+	reinterpret_cast<d4 *>(y)[c] = d4{dv * xv.x + (-(0.0 + a[0]) + rv.x) / p, dv * xv.y + (-(0.0 + a[1]) + rv.y) / p,
+	                                 dv * xv.z + (-(0.0 + a[2]) + rv.z) / p, dv * xv.w + (-(0.0 + a[3]) + rv.w) / p};
+}
+
 template <int FLUX>
 void launch_face(fv_disc_impl *Dh, const double *u, int getdt, dim3 grid, int bs, cudaStream_t s)
 {
@@ -141,6 +171,23 @@ cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int ge
 	face_launch(Dh, u, gettimesteps, s);
 	const int bc = Dh->bs[KBS_GATHER];
 	k_gather<<<grid_of(D.nelem, bc, Dh->batch), bc, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
+	Dh->kernels_launched += 2;
+	return cudaGetLastError();
+}
+
+/* y = dtm x + (R(up) - R(u)) / pm with up = u + pm x already formed and r = -R(u):
+ * the residual's passes at up with the matrix-free finish fused into the gather */
+cudaError_t residual_mf_launch(fv_disc_impl *Dh, const double *up, const double *x, const double *r, const double *dtm,
+                               const double *pm, double *y, cudaStream_t s)
+{
+	const DiscDev &D = Dh->d;
+	if (D.order2) {
+		const cudaError_t e = gradient_pass_launch(Dh, up, s);
+		if (e) return e;
+	}
+	face_launch(Dh, up, 0, s);
+	const int bc = Dh->bs[KBS_GATHER];
+	k_gather_mf<<<grid_of(D.nelem, bc, Dh->batch), bc, 0, s>>>(D, Dh->w, x, r, dtm, pm, y);
 	Dh->kernels_launched += 2;
 	return cudaGetLastError();
 }

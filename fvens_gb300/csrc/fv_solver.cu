@@ -193,16 +193,14 @@ __global__ void k_init(int B, StepState S, const int *__restrict__ mask)
 }
 
 /* matrix-free product pieces (alinalg.cpp:143-237) */
-__global__ void __launch_bounds__(RBS) k_mf_prep(size_t n, int nblk_unused, const double *__restrict__ u,
-                                                 const double *__restrict__ x, const double *__restrict__ pm,
-                                                 double *__restrict__ aux, double *__restrict__ yg, const int *active)
+__global__ void __launch_bounds__(RBS) k_mf_prep(size_t n, const double *__restrict__ u, const double *__restrict__ x,
+                                                 const double *__restrict__ pm, double *__restrict__ aux, const int *active)
 {
 	const int b = blockIdx.y;
 	if (active && !active[b]) return;
 	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= n) return;
 	aux[b * n + e] = u[b * n + e] + pm[b] * x[b * n + e];
-	yg[b * n + e] = 0.0;
 }
 
 __global__ void k_mf_pm(int B, int nblk, const double *__restrict__ part, double eps, double *__restrict__ pm,
@@ -214,18 +212,6 @@ __global__ void k_mf_pm(int B, int nblk, const double *__restrict__ part, double
 	for (int k = threadIdx.x; k < nblk; k += 32) s += part[(size_t)b * nblk + k];
 	for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
 	if (threadIdx.x == 0) pm[b] = eps / sqrt(s);
-}
-
-__global__ void k_mf_finish(int N, const double *__restrict__ x, const double *__restrict__ r,
-                            const double *__restrict__ yg, const double *__restrict__ dtm,
-                            const double *__restrict__ pm, double *__restrict__ y, const int *active)
-{
-	const int b = blockIdx.y;
-	if (active && !active[b]) return;
-	const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-	if (e >= (size_t)N * 4) return;
-	const size_t k = (size_t)b * N * 4 + e;
-	y[k] = dtm[(size_t)b * N + e / 4] * x[k] + (-yg[k] + r[k]) / pm[b];
 }
 
 __global__ void __launch_bounds__(RBS) k_sq_partial(int n, int nblk, const double *__restrict__ x,
@@ -259,7 +245,7 @@ struct MatrixOp : LinOp {
 struct MatrixFreeOp : LinOp {
 	fv_disc_impl *D;
 	const double *u, *r, *dtm;
-	double *aux, *yg, *pm, *part;
+	double *aux, *pm, *part;
 	int nblk;
 	double eps;
 	cudaError_t apply(const double *x, double *y, const int *active, cudaStream_t s, int *nk) override
@@ -268,18 +254,17 @@ struct MatrixFreeOp : LinOp {
 		const int n = 4 * N;
 		k_sq_partial<<<dim3(nblk, B), RBS, 0, s>>>(n, nblk, x, part, active);
 		k_mf_pm<<<B, 32, 0, s>>>(B, nblk, part, eps, pm, active);
-		k_mf_prep<<<dim3((n + 255) / 256, B), 256, 0, s>>>((size_t)n, nblk, u, x, pm, aux, yg, active);
+		k_mf_prep<<<dim3((n + 255) / 256, B), 256, 0, s>>>((size_t)n, u, x, pm, aux, active);
 		*nk += 3;
 		const int *saved = D->d.active;
 		D->d.active = active;
 		const int before = D->kernels_launched;
-		cudaError_t e = residual_launch(D, aux, yg, 0, nullptr, s);
+		// residual at u + pm x with y = dtm x + (R(u + pm x) - R(u)) / pm formed in its gather
+		cudaError_t e = residual_mf_launch(D, aux, x, r, dtm, pm, y, s);
 		*nk += D->kernels_launched - before;
 		D->kernels_launched = before;
 		D->d.active = saved;
 		if (e) return e;
-		k_mf_finish<<<dim3((n + 255) / 256, B), 256, 0, s>>>(N, x, r, yg, dtm, pm, y, active);
-		*nk += 1;
 		return cudaGetLastError();
 	}
 };
@@ -304,7 +289,7 @@ struct fv_solver {
 	Krylov K;
 	StepState S;
 	double *r = nullptr, *du = nullptr, *dtm = nullptr, *part = nullptr;
-	double *aux = nullptr, *yg = nullptr, *mfpart = nullptr;
+	double *aux = nullptr, *mfpart = nullptr;
 	int nblk = 1;
 	std::vector<void *> owned;
 	cudaGraphExec_t exec = nullptr;
@@ -527,7 +512,6 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	if (!e) e = salloc(S, &S->S.hist, 3 * (size_t)cfg->max_timesteps * B);
 	if (!e && cfg->matrix_free) {
 		e = salloc(S, &S->aux, 4 * (size_t)N * B);
-		if (!e) e = salloc(S, &S->yg, 4 * (size_t)N * B);
 		if (!e) e = salloc(S, &S->mfpart, (size_t)S->nblk * B);
 	}
 	if (e) {
@@ -540,7 +524,6 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	S->mfop.r = S->r;
 	S->mfop.dtm = S->dtm;
 	S->mfop.aux = S->aux;
-	S->mfop.yg = S->yg;
 	S->mfop.pm = S->S.pm;
 	S->mfop.part = S->mfpart;
 	S->mfop.nblk = S->nblk;
