@@ -258,6 +258,7 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(m, s1, s2, args.cpu_seconds)
+        line["oracle_parity"] = oracle_parity(m, main, u_conv)
     if rank == 0:
         print(json.dumps(line), flush=True)
     reps.close()
@@ -550,6 +551,31 @@ def _oracle_step_model(od, cfg, u, budget_s):
     t8 = _oracle_steps(od, cfg, u, n, 8)
     b = max((t8 - t1) / 7.0, 0.0)
     return t1 - b, b, n
+
+
+def oracle_parity(m, main, ud):
+    """The GPU's numbers on this workload against the oracle on the same mesh and
+    state: the second-order residual at the converged state and at a seeded
+    5 % perturbation of freestream (max |difference| over the largest sum of
+    |face flux x length| of a cell), and Cl, CDp at the converged state."""
+    import torch
+    from oracle import orc
+    _, od2 = _oracle_case(m)
+    out = {}
+    u_conv = ud.detach().cpu().numpy().reshape(m.nelem, 4)
+    rng = np.random.default_rng(1234)
+    u_pert = np.tile(od2.freestream(), (m.nelem, 1)) * (1 + 0.05 * rng.uniform(-1, 1, (m.nelem, 4)))
+    for tag, u in (("converged", u_conv), ("perturbed", u_pert)):
+        udev = torch.tensor(u, device=ud.device)
+        r = torch.zeros_like(udev)
+        main.compute_residual(udev, r)
+        main.synchronize()
+        ro, _ = od2.residual(u)
+        out[f"residual_{tag}_max_rel_err"] = float(np.abs(r.cpu().numpy() - ro).max() / od2.flux_scale(u).max())
+    cg = main.surface_data(ud, 2)[0]
+    co = od2.surface_data(u_conv, 2)
+    out["cl_cdp_rel_err"] = [float(abs(cg[k] - co[k]) / abs(co[k])) for k in (0, 1)]
+    return out
 
 
 def cpu_baseline(m, starter, main, budget_s):
