@@ -280,3 +280,39 @@ def test_hybrid_naca_generator_quality():
     assert np.hypot(X[far, 0] - 0.5, X[far, 1]).min() >= 20.0
     with pytest.raises(fv.FvensError):
         fv.UMesh.generate(fv.MESH_NACA_HYBRID, [512, 48, 1e-4, 1.12, 20.0, 1.5])
+
+
+_SQ = [[0, 0], [1, 0], [0, 1], [1, 1]]
+
+
+def _mesh(coords, nnode, inpoel, bface, btag):
+    return fv.UMesh.from_arrays(np.array(coords, float), np.array(nnode, np.int32), np.array(inpoel, np.int32),
+                                np.array(bface, np.int32), np.array(btag, np.int32))
+
+
+def test_smallest_meshes_and_orientation():
+    """One triangle (all faces on the boundary), a clockwise triangle (flipped,
+    as preprocessMesh does), two triangles sharing one interior face."""
+    m = _mesh(_SQ[:3], [3], [[0, 1, 2, -1]], [[0, 1], [1, 2], [2, 0]], [1, 1, 1])
+    assert (m.nelem, m.nbface, m.naface) == (1, 3, 3) and m.geometry()["area"][0] == 0.5
+    m = _mesh(_SQ[:3], [3], [[0, 2, 1, -1]], [[0, 1], [1, 2], [2, 0]], [1, 1, 1])
+    assert m.geometry()["area"][0] == 0.5
+    m = _mesh(_SQ, [3, 3], [[0, 1, 3, -1], [0, 3, 2, -1]], [[0, 1], [1, 3], [3, 2], [2, 0]], [1, 1, 1, 1])
+    assert (m.nelem, m.nbface, m.naface) == (2, 4, 5)
+
+
+@pytest.mark.parametrize("coords,nnode,inpoel,bface,what", [
+    (_SQ, [3, 3], [[0, 1, 3, -1], [0, 3, 2, -1]], [[0, 1], [1, 3], [3, 2]], "number of boundary faces"),
+    (_SQ, [3, 3], [[0, 1, 3, -1], [0, 3, 2, -1]], [[0, 1], [1, 3], [3, 2], [2, 1]], "not an edge"),
+    ([[0, 0], [1, 0], [2, 0]], [3], [[0, 1, 2, -1]], [[0, 1], [1, 2], [2, 0]], "non-positive area"),
+    (_SQ, [3, 3], [[0, 1, 3, -1], [0, 3, 7, -1]], [[0, 1], [1, 3], [3, 2], [2, 0]], "out of range"),
+    ([[0, 0], [1, 0], [0.5, 1], [0.5, -1], [0.5, 0.5]], [3, 3, 3],
+     [[0, 1, 2, -1], [0, 3, 1, -1], [0, 1, 4, -1]], [[1, 2], [2, 0], [0, 3], [3, 1], [1, 4], [4, 0]],
+     "non-manifold"),
+    (_SQ, [5], [[0, 1, 3, 2]], [[0, 1], [1, 3], [3, 2], [2, 0]], "triangles and quadrilaterals"),
+], ids=["missing_boundary_face", "stray_boundary_face", "degenerate_cell", "bad_node_index", "non_manifold_edge",
+        "bad_cell_kind"])
+def test_invalid_meshes_are_rejected(coords, nnode, inpoel, bface, what):
+    with pytest.raises(fv.FvensError, match=what) as e:
+        _mesh(coords, nnode, inpoel, bface, [1] * len(bface))
+    assert e.value.status == fv.FV_ERR_MESH
