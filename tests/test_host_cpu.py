@@ -316,3 +316,29 @@ def test_invalid_meshes_are_rejected(coords, nnode, inpoel, bface, what):
     with pytest.raises(fv.FvensError, match=what) as e:
         _mesh(coords, nnode, inpoel, bface, [1] * len(bface))
     assert e.value.status == fv.FV_ERR_MESH
+
+
+def test_disc_and_network_argument_checks():
+    """Argument checks that return before any device work: no batch members,
+    an unknown scheme index, the periodic BC (not implemented by the
+    reference's flow discretisation), a boundary marker without a BC, and a
+    warm-start network without layers."""
+    import ctypes
+    m = cases.channel(8, 4)
+    num = fv.numerics_cfg(flux="ROE")
+    with pytest.raises(fv.FvensError) as e:
+        fv.FlowFV(m, [], num, cases.CHANNEL_BCS)
+    assert e.value.status == fv.FV_ERR_INVALID
+    bad = fv.numerics_cfg(flux="ROE")
+    bad.conv_numflux = 9
+    with pytest.raises(fv.FvensError) as e:
+        fv.FlowFV(m, fv.physics_cfg(Minf=0.5), bad, cases.CHANNEL_BCS)
+    assert e.value.status == fv.FV_ERR_INVALID
+    with pytest.raises(fv.FvensError) as e:
+        fv.FlowFV(m, fv.physics_cfg(Minf=0.5), num, [(1, "periodic", ())] + cases.CHANNEL_BCS[1:])
+    assert e.value.status == fv.FV_ERR_UNSUPPORTED
+    with pytest.raises(fv.FvensError, match="no boundary condition for boundary marker 4") as e:
+        fv.FlowFV(m, fv.physics_cfg(Minf=0.5), num, cases.CHANNEL_BCS[:3])
+    assert e.value.status == fv.FV_ERR_INVALID
+    h = ctypes.c_void_p()
+    assert fv.lib().fv_mpnn_create(m._h, 0, None, 0, ctypes.c_ulonglong(1), ctypes.byref(h)) == fv.FV_ERR_INVALID
