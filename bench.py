@@ -382,7 +382,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
     against one plain FP64 solve."""
     import collections
 
-    from fvens_gb300.mpnn import MPNN, output_scale, train
+    from fvens_gb300.mpnn import MPNN, fallback_solve, output_scale, train
     m, _ = _laminar_mesh(fv)
     phs_tr = _laminar_conditions(fv, n_train, 11)
     phs_te = _laminar_conditions(fv, n_test, 12)
@@ -417,6 +417,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
            "epochs": epochs, "train_batch": 16, "params": net.nparams, "data_generation_s": gen_s,
            "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
     agg = {k: dict(seconds=0.0, steps=[], res0=[], status=collections.Counter()) for k in ("freestream", "warm")}
+    fb = dict(seconds=0.0, members=0, converged=0)
     err_ratio, du, dcl, dcd, pred_s = [], [], [], [], 0.0
     for s in range(0, n_test, B):
         plist = phs_te[s:s + B]
@@ -437,6 +438,21 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
         u0_warm = u_warm.clone()
         t, st_warm = _timed_solve(torch, solvers_w, u_warm, all_members=True)
         agg["warm"]["seconds"] += t + a.elapsed_time(b) / 1e3
+        # the network's result judged: members that did not converge restart from freestream
+        st_fb = [dict(x) for x in st_warm]
+        starter_fb = fv.SteadyBackwardEulerSolver(
+            fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS), cfl_min=200,
+            cfl_max=1000, tolerance=1e-1, abs_tolerance=0, max_timesteps=50, pc="ilu0", nl_update=2, precision=4)
+        u_fb = u_warm.clone()
+        a2, b2 = ev(), ev()
+        a2.record()
+        fell = fallback_solve(main_w, starter_fb, solvers_w[-1], u_fb, st_fb)
+        b2.record()
+        torch.cuda.synchronize()
+        fb["seconds"] += a2.elapsed_time(b2) / 1e3
+        fb["members"] += len(fell)
+        fb["converged"] += sum(1 for x in st_fb if x["status"] == 0)
+        del starter_fb
         # freestream stats from the main solver (the starter's steps added)
         for tag, sts in (("freestream", st_free), ("warm", st_warm)):
             agg[tag]["status"].update(int(x["status"]) for x in sts)
@@ -469,6 +485,10 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
                     "status_counts": {str(k): v for k, v in st["status"].items()}}
     out["freestream"]["note"] = "main-solve steps; a first-order starter ran before each batch"
     out["warm"]["prediction_s"] = pred_s
+    # with the fallback: the members the warm start did not converge, solved again from freestream
+    fb_s = out["warm"]["seconds"] + fb["seconds"]
+    out["warm_with_fallback"] = {"seconds": fb_s, "converged": fb["converged"], "fallback_members": fb["members"],
+                                 "fallback_s": fb["seconds"], "converged_solves_s": fb["converged"] / fb_s}
     out["initial_error_ratio_mean"] = float(np.mean(err_ratio)) if err_ratio else None
     out["initial_error_ratio_max"] = float(np.max(err_ratio)) if err_ratio else None
     # both starts converged: how far apart are the two converged states?

@@ -146,3 +146,35 @@ def train(net, phys, states, epochs, batch, lr, seed=0, lr_final=None, log=None)
         if log:
             log(ep, losses[-1])
     return losses
+
+
+def fallback_solve(main, start_solver, main_solver, u, stats):
+    """The fallback of a warm-started batch: members whose solve did not
+    converge (stats[k]["status"] != 0) restart from freestream with the starter
+    and the main solve (the method without the network); the others keep
+    their states.  Updates stats in place; returns the members that fell back."""
+    import torch
+    failed = [k for k, st in enumerate(stats) if st["status"] != 0]
+    if failed:
+        mask = np.zeros(len(stats), np.int32)
+        mask[failed] = 1
+        uv = u.view(len(stats), -1, 4)
+        free = torch.tensor(main.freestream(), device=u.device, dtype=u.dtype)
+        for k in failed:
+            uv[k] = free[k]
+        start_solver.solve(u, member_mask=mask, raise_on_error=False)
+        _, again = main_solver.solve(u, member_mask=mask, raise_on_error=False)
+        for k in failed:
+            stats[k] = dict(again[k], fallback=True)
+    return failed
+
+
+def warm_started_solve(net, phys, main, start_solver, main_solver, u):
+    """Solves the conditions `phys` from the network's prediction and judges
+    the result: the main solve runs from the prediction, and members that do
+    not converge fall back to freestream with the starter (fallback_solve).
+    u: device array of the batch (filled here).  Returns (stats per member,
+    members that fell back)."""
+    net.predict(phys, u)
+    _, stats = main_solver.solve(u, raise_on_error=False)
+    return stats, fallback_solve(main, start_solver, main_solver, u, stats)

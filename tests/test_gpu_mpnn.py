@@ -134,3 +134,35 @@ def test_warm_start_gains_over_freestream(cuda):
     # same converged state (both at ||R|| < 1e-10)
     assert np.abs(u_warm.cpu().numpy() - ref).max() <= 1e-8 * np.abs(ref).max()
     assert sum(steps_warm) < sum(steps_free), (steps_warm, steps_free)
+
+
+def test_warm_started_solve_falls_back_to_freestream(cuda):
+    """A prediction the solver cannot converge from (an untrained network with
+    a huge output scale) is judged and replaced: the member restarts from
+    freestream with the starter and ends at the state of the method without
+    the network."""
+    import torch
+
+    from fvens_gb300.mpnn import warm_started_solve
+    m = cases.channel(24, 8)
+    phys, _ = _conds([0.45, 0.55])
+    num = fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES")
+    main = fv.FlowFV(m, phys, num, cases.CHANNEL_BCS)
+    start = fv.FlowFV(m, phys, fv.numerics_cfg(flux="ROE", gradient="NONE"), cases.CHANNEL_BCS)
+    cfg = dict(cfl_min=10, cfl_max=1000, tolerance=1e-10, abs_tolerance=1, max_timesteps=300, pc="ilu0")
+    S_main = fv.SteadyBackwardEulerSolver(main, **cfg)
+    S_start = fv.SteadyBackwardEulerSolver(start, cfl_min=10, cfl_max=500, tolerance=1e-1, abs_tolerance=0,
+                                           max_timesteps=20, pc="ilu0")
+    net = MPNN(m, layers=2, seed=4)
+    _random_params(net, 5, amp=1.0)
+    net.set_scale(np.array([50.0, 50.0, 50.0, 50.0], np.float32))
+    u = torch.zeros((2 * m.nelem, 4), dtype=torch.float64, device=cuda)
+    stats, fell = warm_started_solve(net, phys, main, S_start, S_main, u)
+    assert fell and all(st["status"] == 0 for st in stats)
+    # the method without the network, from freestream
+    u_ref = torch.tensor(np.repeat(main.freestream()[:, None, :], m.nelem, axis=1).reshape(-1, 4), device=cuda)
+    S_start.solve(u_ref, raise_on_error=False)
+    S_main.solve(u_ref)
+    ug, ur = u.view(2, -1, 4).cpu().numpy(), u_ref.view(2, -1, 4).cpu().numpy()
+    for k in fell:
+        assert np.abs(ug[k] - ur[k]).max() <= 1e-8 * np.abs(ur[k]).max()
