@@ -342,3 +342,19 @@ def test_disc_and_network_argument_checks():
     assert e.value.status == fv.FV_ERR_INVALID
     h = ctypes.c_void_p()
     assert fv.lib().fv_mpnn_create(m._h, 0, None, 0, ctypes.c_ulonglong(1), ctypes.byref(h)) == fv.FV_ERR_INVALID
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF_MESHES, "testanisotropic-lines.txt")),
+                    reason="reference test inputs not present")
+def test_find_lines_matches_reference_golden_lines():
+    """tests/mesh/testlineordering.cpp (MeshUtils_findLines_smallmesh): on
+    testanisotropic.msh with threshold 10 the lines are the cells of
+    testanisotropic-lines.txt (Gmsh element numbers, boundary elements first)."""
+    m = fv.UMesh.read_gmsh(os.path.join(REF_MESHES, "testanisotropic.msh"), reorder=0)
+    nl, cl = m.find_lines(10.0)
+    gold = [[int(c) - m.nbface - 1 for c in ln.split()]
+            for ln in open(os.path.join(REF_MESHES, "testanisotropic-lines.txt")) if ln.strip()]
+    assert nl == len(gold)
+    for k, cells in enumerate(gold):
+        assert [int(cl[c]) for c in cells] == [k] * len(cells)
+    assert int((cl >= 0).sum()) == sum(len(g) for g in gold)
