@@ -185,3 +185,24 @@ def test_matrix_free_solve_matches_oracle(cuda):
     assert abs(st[0]["steps"] - sto["steps"]) <= 2
     ug = ud.cpu().numpy()
     assert np.abs(ug - uo).max() / np.abs(uo).max() <= 1e-8
+
+
+def test_matrix_free_first_order_matches_matrix_based(cuda):
+    """The reference's Flow_Euler_Cylinder_HLLC_MatFreeVsMat
+    (tests/solvers/testmatrixfree.cpp, matfree.ctrl): for a first-order HLLC
+    discretisation the stored Jacobian is the residual's exact derivative, so
+    the matrix-free solve (difference step 1e-6) takes the steps of the
+    matrix-based one (M 0.38, CFL 50 -> 3000, relative tolerance 1e-8, FGMRES
+    rtol 1e-2; here on the NACA 0012 O-grid with ILU(0))."""
+    import torch
+    m = cases.naca()
+    d = fv.FlowFV(m, fv.physics_cfg(Minf=0.38), fv.numerics_cfg(flux="HLLC", gradient="NONE"), cases.NACA_INV_BCS)
+    cfg = dict(cfl_min=50, cfl_max=3000, tolerance=1e-8, abs_tolerance=0, max_timesteps=100, pc="ilu0", precision=8,
+               ksp_rtol=1e-2)
+    u0 = torch.tensor(np.tile(d.freestream()[0], (m.nelem, 1)), device=cuda)
+    ua, ub = u0.clone(), u0.clone()
+    _, sa = fv.SteadyBackwardEulerSolver(d, **cfg).solve(ua)
+    _, sb = fv.SteadyBackwardEulerSolver(d, matrix_free=1, mf_eps=1e-6, **cfg).solve(ub)
+    assert sa[0]["status"] == 0 and sb[0]["status"] == 0
+    assert abs(sa[0]["steps"] - sb[0]["steps"]) <= 1, (sa[0]["steps"], sb[0]["steps"])
+    assert (ua - ub).abs().max().item() <= 1e-6 * ua.abs().max().item()
