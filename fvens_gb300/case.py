@@ -19,7 +19,6 @@ leaves it unset); implicit pseudo-time only (explicit cases go through
 """
 import argparse
 import math
-import os
 import shlex
 import sys
 import time
@@ -176,9 +175,9 @@ class FlowParserOptions:
         return [(marker, typ, vals) for (marker, typ, vals) in self.bcconf]
 
 
-_LIMITERS = {"NONE": "NONE", "VANALBADA": "VANALBADA", "BARTHJESPERSEN": "BARTHJESPERSEN",
-             "VENKATAKRISHNAN": "VENKATAKRISHNAN", "WENO": "WENO"}
-_GRADIENTS = {"NONE": "NONE", "LEASTSQUARES": "LEASTSQUARES", "GREENGAUSS": "GREENGAUSS"}
+# scheme names of the control file (afactory.cpp:103-227)
+_LIMITERS = ("NONE", "VANALBADA", "BARTHJESPERSEN", "VENKATAKRISHNAN", "WENO")
+_GRADIENTS = ("NONE", "LEASTSQUARES", "GREENGAUSS")
 # boundary-condition names of the control file (bcTypeMap, src/spatial/abctypemap.cpp:16-30)
 _BC_NAMES = ("slipwall", "isothermalwall", "adiabaticwall", "farfield", "inflowoutflow", "subsonic_inflow",
              "extrapolation", "periodic")
