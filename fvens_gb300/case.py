@@ -390,13 +390,29 @@ class SteadyFlowCase:
         start = fv.FlowFV(m, self.physics(), num1, o.bcconf_tuples()) if o.usestarter else None
         return main, start
 
-    def execute(self, m, u=None, log=print):
+    def execute(self, m, u=None, log=print, net=None):
         """Starter (Tolerance errors ignored) and main solve on the device
-        state u (freestream when None).  Returns (u, main stats, starter stats,
-        main solver)."""
+        state u (freestream when None).  With a warm-start network `net` the
+        main solve starts from its prediction instead, and falls back to
+        freestream + starter when it does not converge.  Returns (u, main
+        stats, starter stats, main solver, discretisation)."""
         import torch
         o = self.opts
         main, start = self.discretisations(m)
+        if net is not None:
+            from .mpnn import warm_started_solve
+            u = torch.empty((m.nelem, 4), dtype=torch.float64, device="cuda")
+            S2 = self._solver(main, o.initcfl, o.endcfl, o.tolerance, o.maxiter)
+            if start is None:
+                start = self.fv.FlowFV(m, self.physics(), self.fv.numerics_cfg(
+                    flux=o.invflux, flux_jac=o.invfluxjac, gradient="NONE", limiter_param=1.0, order2=False),
+                    o.bcconf_tuples())
+            S1 = self._solver(start, o.firstinitcfl or o.initcfl, o.firstendcfl or o.endcfl,
+                              o.firsttolerance or 1e-1, o.firstmaxiter or 50)
+            stats, fell = warm_started_solve(net, [self.physics()], main, S1, S2, u)
+            log(f"SteadyFlowCase: warm start, main {stats[0]['steps']} steps, status {stats[0]['status']}"
+                + (" (fell back to freestream)" if fell else ""))
+            return u, stats[0], None, S2, main
         if u is None:
             u = torch.tensor(np.tile(main.freestream()[0], (m.nelem, 1)), device="cuda")
         st1 = None
@@ -414,13 +430,14 @@ class SteadyFlowCase:
             f"status {st2['status']}, residual {st2['res']:.3e}")
         return u, st2, st1, S2, main
 
-    def run_output(self, m=None, surface_files=True, log=print):
-        """FlowCase::run_output (casesolvers.cpp:86-164): solve, write the
-        convergence history and surface files, return the functionals."""
+    def run_output(self, m=None, surface_files=True, log=print, net=None):
+        """FlowCase::run_output (casesolvers.cpp:86-164): solve (from the
+        network's prediction when `net` is given), write the convergence
+        history and surface files, return the functionals."""
         o = self.opts
         m = m or self.read_mesh()
         t0 = time.perf_counter()
-        u, st, st1, S, main = self.execute(m, log=log)
+        u, st, st1, S, main = self.execute(m, log=log, net=net)
         wall = time.perf_counter() - t0
         if st["status"] == self.fv.FV_ERR_NUMERICAL:
             raise self.fv.FvensError(st["status"], "main flow solve failed (non-finite residual)")
@@ -445,10 +462,17 @@ def main(argv=None):
     ap.add_argument("--mesh_file", default=None)
     ap.add_argument("--precision", type=int, default=4, choices=[4, 8],
                     help="stored Jacobian / preconditioner precision (4: FP32, 8: FP64)")
+    ap.add_argument("--warm-start", default=None,
+                    help="trained network (.npz from fvens_gb300.mpnn.MPNN.save) predicting the initial state")
     a = ap.parse_args(argv)
     opts = parse_flow_controlfile(a.control_file, a.mesh_file)
     case = SteadyFlowCase(opts, parse_solver_options(a.options), precision=a.precision)
-    f, st = case.run_output()
+    m = case.read_mesh()
+    net = None
+    if a.warm_start:
+        from .mpnn import MPNN
+        net = MPNN.load(m, a.warm_start)
+    f, st = case.run_output(m, net=net)
     print(f"h {f.h:.6g} entropy {f.entropy:.6g} Cl {f.Cl:.10g} Cdp {f.Cdp:.10g} Cdf {f.Cdf:.10g}")
     return 0 if st["status"] == 0 else 1
 

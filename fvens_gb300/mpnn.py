@@ -47,7 +47,7 @@ class MPNN:
 
     def __init__(self, mesh, layers=4, wall_markers=(), seed=0):
         L = _bind()
-        self.mesh, self.layers = mesh, layers
+        self.mesh, self.layers, self.wall_markers = mesh, layers, tuple(wall_markers)
         wm = (ctypes.c_int * max(len(wall_markers), 1))(*wall_markers)
         h = ctypes.c_void_p()
         check(L.fv_mpnn_create(mesh._h, layers, wm, len(wall_markers), seed, ctypes.byref(h)))
@@ -104,6 +104,23 @@ class MPNN:
         loss = ctypes.c_float()
         check(_bind().fv_mpnn_train_step(self._h, arr, b, _vp(dptr(target)), float(lr), ctypes.byref(loss)))
         return float(loss.value)
+
+    def save(self, path):
+        """Writes the trained network (parameters, output scale, layers, wall
+        markers and the mesh's cell count) to an .npz file."""
+        np.savez(path, params=self.params(), scale=self.scale, layers=self.layers,
+                 wall_markers=np.asarray(self.wall_markers, np.int32), nelem=self.mesh.nelem)
+
+    @classmethod
+    def load(cls, mesh, path):
+        """A network written by save(), on the same mesh."""
+        z = np.load(path)
+        if int(z["nelem"]) != mesh.nelem:
+            raise ValueError(f"network was trained on a mesh of {int(z['nelem'])} cells, not {mesh.nelem}")
+        net = cls(mesh, layers=int(z["layers"]), wall_markers=tuple(int(x) for x in z["wall_markers"]))
+        net.params(z["params"])
+        net.set_scale(z["scale"])
+        return net
 
     def __del__(self):
         if getattr(self, "_h", None) is not None:

@@ -49,3 +49,29 @@ def test_control_file_case_matches_direct_solve(cuda, tmp_path, monkeypatch):
     w1 = open("channel-surf_w1.out").read().splitlines()
     assert w1[0].startswith("#  x") and w1[-2] == "# Cl      Cdp      Cdf"
     assert len(w1) - 3 == int((mr.export()["btag"] == 1).sum())
+
+
+def test_control_file_case_with_warm_start_network(cuda, tmp_path, monkeypatch):
+    """The case runner with a warm-start network (saved and loaded again):
+    the main solve starts from the prediction (or falls back to freestream)
+    and reaches the functionals of the freestream-started case."""
+    from fvens_gb300.mpnn import MPNN
+    m = cases.channel(48, 16)
+    cases.write_gmsh(m, str(tmp_path / "channel.msh"))
+    shutil.copy(os.path.join(GOLDEN, "channel_case.ctrl"), tmp_path / "channel_case.ctrl")
+    monkeypatch.chdir(tmp_path)
+    opts = case.parse_flow_controlfile("channel_case.ctrl")
+    so = case.parse_solver_options(os.path.join(GOLDEN, "channel_opts.solverc"))
+    c = case.SteadyFlowCase(opts, so)
+    mr = c.read_mesh()
+    f_free, st_free = c.run_output(mr, surface_files=False, log=lambda *a: None)
+    net = MPNN(mr, layers=2, wall_markers=(1, 3), seed=2)
+    p = net.params((np.random.default_rng(0).normal(size=net.nparams) * 0.1).astype(np.float32))
+    net.set_scale(np.array([0.01, 0.01, 0.01, 0.02], np.float32))
+    net.save(str(tmp_path / "net.npz"))
+    net2 = MPNN.load(mr, str(tmp_path / "net.npz"))
+    assert np.array_equal(net2.params(), p) and np.array_equal(net2.scale, net.scale)
+    f_warm, st_warm = c.run_output(mr, surface_files=False, log=lambda *a: None, net=net2)
+    assert st_free["status"] == 0 and st_warm["status"] == 0
+    assert abs(f_warm.Cl - f_free.Cl) <= 1e-6 * max(abs(f_free.Cl), 1e-3)
+    assert abs(f_warm.Cdp - f_free.Cdp) <= 1e-6 * max(abs(f_free.Cdp), 1e-3)
