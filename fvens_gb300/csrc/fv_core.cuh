@@ -120,9 +120,11 @@ cudaError_t residual_launch(fv_disc_impl *D, const double *u, double *r, int get
 cudaError_t gradients_launch(fv_disc_impl *D, const double *u, double *grad, int conserved, cudaStream_t s);
 /* the residual's passes before the face kernel (primitive/ghost states,
  * gradients, limiter values, WENO blend) into the handle's scratch */
-cudaError_t gradient_pass_launch(fv_disc_impl *D, const double *u, cudaStream_t s);
-cudaError_t residual_mf_launch(fv_disc_impl *D, const double *up, const double *x, const double *r, const double *dtm,
-                               const double *pm, double *y, cudaStream_t s);
+/* the passes before the face kernel; with x, at the state u + pm x (per member pm) */
+cudaError_t gradient_pass_launch(fv_disc_impl *D, const double *u, cudaStream_t s, const double *x = nullptr,
+                                 const double *pm = nullptr);
+cudaError_t residual_mf_launch(fv_disc_impl *D, const double *u, const double *up, const double *x, const double *r,
+                               const double *dtm, const double *pm, double *y, cudaStream_t s);
 /* times the residual kernels at 64 / 128 / 256 threads per block at state u
  * and keeps the fastest per kernel in D->bs; chosen[4] (may be NULL) receives them */
 cudaError_t residual_autotune(fv_disc_impl *D, const double *u, cudaStream_t s, int *chosen);

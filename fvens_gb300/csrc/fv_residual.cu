@@ -29,6 +29,44 @@ __global__ void __launch_bounds__(kMaxBS) k_prep(DiscDev D, const double *__rest
 	prep_body(D, b, blockIdx.x * blockDim.x + threadIdx.x, u, w);
 }
 
+/* k_prep at the matrix-free product's perturbed state u + pm x, formed on the
+ * fly (the same sum the separate perturbation kernel stores) */
+__global__ void __launch_bounds__(kMaxBS) k_prep_mf(DiscDev D, const double *__restrict__ u,
+                                                    const double *__restrict__ x, const double *__restrict__ pm,
+                                                    ResidualWork w)
+{
+	const int b = blockIdx.y;
+	if (skip_member(D, b)) return;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const Phys &P = D.phys[b];
+	const double p = pm[b];
+	const size_t c0 = (size_t)b * D.nelem;
+	auto state = [&](int i, double *uc) {
+		const d4 a = reinterpret_cast<const d4 *>(u)[c0 + i], v = reinterpret_cast<const d4 *>(x)[c0 + i];
+		uc[0] = a.x + p * v.x;
+		uc[1] = a.y + p * v.y;
+		uc[2] = a.z + p * v.z;
+		uc[3] = a.w + p * v.w;
+	};
+	if (t < D.nelem) {
+		double uc[4], up[4];
+		state(t, uc);
+		prim_of_cons(P, uc, up);
+		w.prim[c0 + t] = d4{up[0], up[1], up[2], up[3]};
+	} else if (t < D.nelem + D.nbface) {
+		const int ib = t - D.nelem;
+		double in[4];
+		state(D.flr[ib].x, in);
+		const d4 g = D.fgeo[ib];
+		const double n[2] = {g.x, g.y};
+		double gs[4], gp[4];
+		ghost_cons<double>(P, D.bcs[D.bcid[ib]], in, n, gs, false);
+		prim_of_cons(P, gs, gp);
+		w.ghost_cons[(size_t)b * D.nbface + ib] = d4{gs[0], gs[1], gs[2], gs[3]};
+		w.ghost_prim[(size_t)b * D.nbface + ib] = d4{gp[0], gp[1], gp[2], gp[3]};
+	}
+}
+
 __global__ void __launch_bounds__(kMaxBS) k_grad(DiscDev D, const d4 *__restrict__ q, const d4 *__restrict__ qg,
                                                  d4 *__restrict__ grad, d4 *__restrict__ phi, int limiter)
 {
@@ -132,13 +170,15 @@ cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cud
 
 /* the residual's passes before the face kernel: primitive and ghost states,
  * gradients (+ Barth-Jespersen / Venkatakrishnan limiter values), WENO blend */
-cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t s)
+cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t s, const double *x,
+                                 const double *pm)
 {
 	const DiscDev &D = Dh->d;
 	const int B = Dh->batch;
 	const int bp = Dh->bs[KBS_PREP], bg = Dh->bs[KBS_GRAD];
 	int nk = 0;
-	k_prep<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, Dh->w);
+	if (x) k_prep_mf<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, x, pm, Dh->w);
+	else k_prep<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, Dh->w);
 	nk++;
 	if (D.gradscheme != GRAD_NONE) {
 		const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
@@ -175,14 +215,17 @@ cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int ge
 	return cudaGetLastError();
 }
 
-/* y = dtm x + (R(up) - R(u)) / pm with up = u + pm x already formed and r = -R(u):
- * the residual's passes at up with the matrix-free finish fused into the gather */
-cudaError_t residual_mf_launch(fv_disc_impl *Dh, const double *up, const double *x, const double *r, const double *dtm,
-                               const double *pm, double *y, cudaStream_t s)
+/* y = dtm x + (R(u + pm x) - R(u)) / pm with r = -R(u): the residual's passes
+ * at the perturbed state with the matrix-free finish fused into the gather.
+ * Second order: the perturbed state is formed inside the first pass (the
+ * later passes read only primitive and ghost states); first order: the face
+ * kernel reads the state, so up = u + pm x must have been stored. */
+cudaError_t residual_mf_launch(fv_disc_impl *Dh, const double *u, const double *up, const double *x,
+                               const double *r, const double *dtm, const double *pm, double *y, cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
 	if (D.order2) {
-		const cudaError_t e = gradient_pass_launch(Dh, up, s);
+		const cudaError_t e = gradient_pass_launch(Dh, u, s, x, pm);
 		if (e) return e;
 	}
 	face_launch(Dh, up, 0, s);

@@ -254,13 +254,16 @@ struct MatrixFreeOp : LinOp {
 		const int n = 4 * N;
 		k_sq_partial<<<dim3(nblk, B), RBS, 0, s>>>(n, nblk, x, part, active);
 		k_mf_pm<<<B, 32, 0, s>>>(B, nblk, part, eps, pm, active);
-		k_mf_prep<<<dim3((n + 255) / 256, B), 256, 0, s>>>((size_t)n, u, x, pm, aux, active);
-		*nk += 3;
+		*nk += 2;
+		if (!D->d.order2) {  // the first-order face kernel reads the perturbed state itself
+			k_mf_prep<<<dim3((n + 255) / 256, B), 256, 0, s>>>((size_t)n, u, x, pm, aux, active);
+			*nk += 1;
+		}
 		const int *saved = D->d.active;
 		D->d.active = active;
 		const int before = D->kernels_launched;
 		// residual at u + pm x with y = dtm x + (R(u + pm x) - R(u)) / pm formed in its gather
-		cudaError_t e = residual_mf_launch(D, aux, x, r, dtm, pm, y, s);
+		cudaError_t e = residual_mf_launch(D, u, aux, x, r, dtm, pm, y, s);
 		*nk += D->kernels_launched - before;
 		D->kernels_launched = before;
 		D->d.active = saved;
