@@ -257,7 +257,8 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(m, s1, s2, args.cpu_seconds)
+        u_host = u_conv.cpu().numpy().reshape(m.nelem, 4)
+        line["cpu_baseline"] = cpu_baseline(m, s1, s2, args.cpu_seconds, u_host)
         line["oracle_parity"] = oracle_parity(m, main, u_conv)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -598,13 +599,15 @@ def oracle_parity(m, main, ud):
     return out
 
 
-def cpu_baseline(m, starter, main, budget_s):
+def cpu_baseline(m, starter, main, budget_s, u_state=None):
     """The oracle (the CPU restatement of the reference's path, natural-order
     ILU(0) as PETSc's) on the host cores: a bounded sample of pseudo-time
     steps of the starter and of the main solve with pinned FGMRES iteration
     counts gives the cost per step and per Krylov iteration, which is applied
     to the step and iteration counts of the GPU solve.  starter / main: the
-    GPU's fv_solve_stats of the two solves."""
+    GPU's fv_solve_stats of the two solves.  With u_state (host array of the
+    state the GPU kernels were timed at), the oracle's residual, FP64 Jacobian
+    assembly, ILU(0) factorisation and ILU(0) apply are timed there too."""
     from oracle import orc
     nthreads = os.cpu_count() or 1
     orc.set_threads(nthreads)
@@ -613,11 +616,19 @@ def cpu_baseline(m, starter, main, budget_s):
     a1, b1, n1 = _oracle_step_model(od1, STARTER, u0, 0.4 * budget_s)
     a2, b2, n2 = _oracle_step_model(od2, MAIN, u0, 0.6 * budget_s)
     solve_s = (a1 * starter["steps"] + b1 * starter["lin_iters"]) + (a2 * main["steps"] + b2 * main["lin_iters"])
+    kernels = {}
+    if u_state is not None:
+        t = od2.time_kernels(u_state, "ilu0", reps=5)
+        kernels = {"kernels_ms": {"residual": 1e3 * t["residual"], "jacobian": 1e3 * t["jacobian"],
+                                  "ilu0_setup": 1e3 * t["pc_setup"], "ilu0_apply": 1e3 * t["pc_apply"]},
+                   "kernels_note": f"oracle at the state the GPU kernels were timed at, median of 5 after one "
+                                   f"untimed call; residual and FP64 Jacobian on {nthreads} threads, ILU(0) "
+                                   f"factorisation and apply sequential in natural order (as PETSc's)"}
     return {"value": 1.0 / solve_s, "unit": "solves/s", "cores": nthreads, "kind": "port",
             "sample": f"2 x {n1} starter + 2 x {n2} main pseudo-time steps of the same workload on the oracle with "
                       f"1 and 8 FGMRES(30) iterations per step (natural-order ILU(0)); per step {a1:.3f} / {a2:.3f} s "
                       f"+ per Krylov iteration {b1:.3f} / {b2:.3f} s, applied to {starter['steps']} + {main['steps']} "
-                      f"steps and {starter['lin_iters']} + {main['lin_iters']} Krylov iterations per solve"}
+                      f"steps and {starter['lin_iters']} + {main['lin_iters']} Krylov iterations per solve", **kernels}
 
 
 def run_reference(args):

@@ -227,6 +227,17 @@ class Disc:
     def entropy_error(self, u):
         return lib().orc_entropy_error(self._h, p(np.ascontiguousarray(u, np.float64)))
 
+    def time_kernels(self, u, pc="ilu0", reps=5):
+        """Median seconds per call of the residual (with local time steps), the
+        Jacobian assembly, the preconditioner setup and one preconditioner
+        apply (natural order) at state u, over `reps` calls after one untimed."""
+        out = np.zeros(4)
+        rc = lib().orc_time_kernels(self._h, p(np.ascontiguousarray(u, np.float64)),
+                                    {"none": 0, "jacobi": 1, "sgs": 2, "ilu0": 3}[pc], int(reps), p(out))
+        if rc:
+            raise RuntimeError(f"oracle kernel timing failed ({rc})")
+        return dict(zip(("residual", "jacobian", "pc_setup", "pc_apply"), out.tolist()))
+
     def __del__(self):
         if getattr(self, "_h", None) is not None and _orc is not None:
             _orc.orc_disc_destroy(self._h)

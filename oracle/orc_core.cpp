@@ -35,6 +35,7 @@
  * cell in ascending face order, so results do not depend on thread count.
  */
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -1365,6 +1366,57 @@ int orc_jacobian(const void *h, const double *u, int *nnzb, int *rowptr, int *co
 	std::memcpy(rowptr, A.rowptr.data(), sizeof(int) * A.rowptr.size());
 	std::memcpy(col, A.col.data(), sizeof(int) * A.col.size());
 	std::memcpy(val, A.val.data(), sizeof(double) * A.val.size());
+	return 0;
+}
+
+/* Median wall time in seconds of `reps` calls (after one untimed call) of each
+ * oracle kernel at state u, on the threads set by orc_set_threads:
+ * out[0] residual with local time steps, out[1] Jacobian assembly into a
+ * zeroed matrix (the zeroing included), out[2] preconditioner setup of type
+ * pctype (0 none, 1 point-block Jacobi, 2 SGS, 3 ILU(0)) in natural order,
+ * out[3] one preconditioner apply.  The CPU-baseline timings of the bench. */
+int orc_time_kernels(const void *h, const double *u, int pctype, int reps, double *out)
+{
+	const Disc *d = (const Disc *)h;
+	if (reps < 1 || pctype < 0 || pctype > 3) return 1;
+	const size_t n = (size_t)d->nelem();
+	using clk = std::chrono::steady_clock;
+	std::vector<double> t(reps + 1);
+	auto timed = [&](auto &&fn) {
+		for (int k = 0; k <= reps; k++) {
+			const auto a = clk::now();
+			if (int e = fn()) return e;
+			t[k] = std::chrono::duration<double>(clk::now() - a).count();
+		}
+		std::sort(t.begin() + 1, t.end());
+		return 0;
+	};
+	std::vector<double> r(4 * n), dt(n), z(4 * n);
+	Disc::Work w;
+	int e = timed([&] {
+		std::fill(r.begin(), r.end(), 0.0);
+		d->residual(u, r.data(), true, dt.data(), w);
+		return 0;
+	});
+	if (e) return e;
+	out[0] = t[1 + reps / 2];
+	BSR A;
+	A.setup(*d->m);
+	if ((e = timed([&] {
+		     std::fill(A.val.begin(), A.val.end(), 0.0);
+		     return assemble_jacobian(*d, u, A);
+	     })))
+		return e;
+	out[1] = t[1 + reps / 2];
+	Precond pc;
+	if ((e = timed([&] { return pc.setup(A, pctype, nullptr); }))) return e;
+	out[2] = t[1 + reps / 2];
+	if ((e = timed([&] {
+		     pc.apply(r.data(), z.data());
+		     return 0;
+	     })))
+		return e;
+	out[3] = t[1 + reps / 2];
 	return 0;
 }
 

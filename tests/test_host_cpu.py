@@ -142,6 +142,21 @@ def test_oracle_solves_small_channel():
     assert np.sqrt((r[:, 3] ** 2 * m.geometry()["area"]).sum()) < 1e-9
 
 
+def test_oracle_kernel_timings():
+    """The CPU baseline's per-kernel timings: every kernel timed, positive,
+    and the timing leaves the oracle's results unchanged."""
+    m = cases.channel(24, 8)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), Minf=0.5, flux="ROE", gradient="LEASTSQUARES",
+                  bcs=cases.CHANNEL_BCS)
+    u = np.tile(od.freestream(), (m.nelem, 1)) * (1 + 1e-3 * np.random.default_rng(1).normal(size=(m.nelem, 4)))
+    r0, _ = od.residual(u)
+    t = od.time_kernels(u, "ilu0", reps=3)
+    assert set(t) == {"residual", "jacobian", "pc_setup", "pc_apply"} and all(v > 0 for v in t.values())
+    assert np.array_equal(od.residual(u)[0], r0)
+    with pytest.raises(RuntimeError):
+        od.time_kernels(u, "ilu0", reps=0)
+
+
 def test_oracle_precond_exact_for_block_diagonal():
     """ILU(0), SGS and Jacobi all invert a block-diagonal matrix exactly."""
     rng = np.random.default_rng(0)
