@@ -2,7 +2,8 @@
 (arrays in tests/golden/, written by tests/golden/make_reference_meshes.py),
 with the control-file settings of the reference's test runs:
   testcases/naca0012/transonic-sanity-test-muscl.ctrl + opts.solverc
-  testcases/visc-naca0012/laminar-implicit.ctrl + opts.solverc"""
+  testcases/visc-naca0012/laminar-implicit.ctrl + opts.solverc
+and the cylinder refinement sequence of tests/inv-2dcyl."""
 import os
 
 import numpy as np
@@ -43,3 +44,25 @@ def load(name):
     m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
                              z["btag"].astype(np.int32), reorder=1)
     return m, c, z["regression"]
+
+
+# The reference's entropy-convergence test on its cylinder refinements
+# (tests/inv-2dcyl: inv-cyl-base.ctrl with inv-cyl-ls-hllc.ctrl or
+# inv-cyl-gg-hllc_tri.ctrl, inv_cyl.solverc): M 0.38, slip wall (marker 2),
+# far field (marker 4), HLLC, no limiter, first-order starter then the
+# second-order main solve, both to a relative tolerance, robust_flow update,
+# -pc_type bjacobi -sub_pc_type ilu
+CYLINDER = dict(
+    bcs=[(2, "slipwall", ()), (4, "farfield", ())], phys=dict(Minf=0.38, aoa_deg=0.0), flux="HLLC",
+    solvers={"LEASTSQUARES": (dict(cfl_min=25, cfl_max=500, tolerance=1e-1, max_timesteps=150),
+                              dict(cfl_min=250, cfl_max=5000, tolerance=1e-5, max_timesteps=300)),
+             "GREENGAUSS": (dict(cfl_min=25, cfl_max=250, tolerance=1e-1, max_timesteps=250),
+                            dict(cfl_min=250, cfl_max=1000, tolerance=1e-5, max_timesteps=350))},
+    pc="ilu0", nl_update="robust_flow")
+
+
+def load_cylinders():
+    """The four meshes 2dcylinder0..3 (RCM-ordered as -mesh_reorder rcm)."""
+    z = np.load(os.path.join(GOLDEN, "2dcylinder_meshes.npz"))
+    return [fv.UMesh.from_arrays(z[f"m{k}_coords"], z[f"m{k}_nnode"].astype(np.int32), z[f"m{k}_inpoel"],
+                                 z[f"m{k}_bface"], z[f"m{k}_btag"].astype(np.int32), reorder=1) for k in range(4)]

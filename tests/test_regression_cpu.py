@@ -43,3 +43,35 @@ def test_oracle_reproduces_laminar_naca0012_regression():
     # CL of the symmetric aerofoil at zero incidence is mesh-asymmetry noise
     # (3e-5): compared in absolute terms
     assert abs(f[0] - regr[0]) <= 1e-7
+
+
+@pytest.mark.parametrize("gradient", ["LEASTSQUARES", "GREENGAUSS"])
+def test_oracle_entropy_convergence_on_reference_cylinders(gradient):
+    """The reference's SpatialFlow_Euler_Cylinder_{LeastSquares,GreenGauss}_HLLC_Tri_EntropyConvergence
+    (tests/flow_conv.cpp:42-89 with tests/inv-2dcyl/*): on 2dcylinder0..3 the
+    starter and main solves of the control files run from freestream; a solve
+    that stops at its step limit is kept, as FlowCase::run_output
+    (casesolvers.cpp:98-103) catches that error; h = 1/sqrt(cells)
+    (casesolvers.cpp:96) and the entropy error of the final state give the
+    orders between refinements, of which the last must lie in [1.65, 2.1].
+    Only that one is checked by the reference, and only the two finest meshes
+    enter it: the oracle's least-squares solves on the two coarsest meshes
+    break down (non-finite residual), as flow_conv.cpp tolerates."""
+    c = rc.CYLINDER
+    s1, s2 = c["solvers"][gradient]
+    logs, statuses = [], []
+    for m in rc.load_cylinders():
+        om = orc.Mesh.from_export(m.export())
+        d1 = orc.Disc(om, **c["phys"], flux=c["flux"], gradient="NONE", bcs=c["bcs"])
+        d2 = orc.Disc(om, **c["phys"], flux=c["flux"], gradient=gradient, bcs=c["bcs"])
+        u0 = np.tile(d2.freestream(), (m.nelem, 1))
+        u1, _ = d1.steady_solve(u0, cflmin=s1["cfl_min"], cflmax=s1["cfl_max"], tol=s1["tolerance"],
+                                maxiter=s1["max_timesteps"], abs_tol=False, pc=c["pc"], nl_update=c["nl_update"])
+        u2, st = d2.steady_solve(u1, cflmin=s2["cfl_min"], cflmax=s2["cfl_max"], tol=s2["tolerance"],
+                                 maxiter=s2["max_timesteps"], abs_tol=False, pc=c["pc"], nl_update=c["nl_update"])
+        statuses.append(st["status"])
+        logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(d2.entropy_error(u2))))
+    # the two finest meshes: converged (0) or stopped at the step limit (6)
+    assert all(s in (0, 6) for s in statuses[2:]), statuses
+    slope = (logs[3][1] - logs[2][1]) / (logs[3][0] - logs[2][0])
+    assert 1.65 <= slope <= 2.1, (slope, logs, statuses)
