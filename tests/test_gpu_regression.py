@@ -89,3 +89,43 @@ def test_entropy_error_converges_at_second_order(cuda, gradient):
         logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(d.entropy_error(u)[0])))
     slope = (logs[-1][1] - logs[-2][1]) / (logs[-1][0] - logs[-2][0])
     assert 1.65 <= slope <= 2.1, (slope, logs)
+
+
+def test_entropy_errors_on_reference_cylinders_match_oracle(cuda):
+    """Green-Gauss HLLC on the reference's cylinder refinements 2dcylinder2 and
+    2dcylinder3 with the settings of its entropy-convergence test
+    (tests/inv-2dcyl), the main solve driven to an absolute residual of 1e-10:
+    the GPU's entropy errors agree with the oracle's converged ones to 1e-8
+    relative, and the order between the two meshes lies in the reference's
+    [1.65, 2.1] (tests/flow_conv.cpp:84-89)."""
+    import torch
+    c = rc.CYLINDER
+    s1, s2 = c["solvers"]["GREENGAUSS"]
+    cfg1 = dict(cfl_min=s1["cfl_min"], cfl_max=s1["cfl_max"], tolerance=s1["tolerance"],
+                max_timesteps=s1["max_timesteps"], pc=c["pc"], nl_update=c["nl_update"])
+    cfg2 = dict(cfl_min=s2["cfl_min"], cfl_max=s2["cfl_max"], tolerance=1e-10, max_timesteps=3000, pc=c["pc"],
+                nl_update=c["nl_update"])
+    logs = []
+    for m in rc.load_cylinders()[2:]:
+        ph = fv.physics_cfg(**c["phys"])
+        start = fv.FlowFV(m, ph, fv.numerics_cfg(flux=c["flux"], gradient="NONE"), c["bcs"])
+        main = fv.FlowFV(m, ph, fv.numerics_cfg(flux=c["flux"], gradient="GREENGAUSS"), c["bcs"])
+        ud = torch.tensor(np.tile(main.freestream()[0], (m.nelem, 1)), device=cuda)
+        fv.SteadyBackwardEulerSolver(start, abs_tolerance=0, precision=4, **cfg1).solve(ud, raise_on_error=False)
+        _, st = fv.SteadyBackwardEulerSolver(main, abs_tolerance=1, precision=4, **cfg2).solve(ud)
+        assert st[0]["status"] == 0 and st[0]["res"] <= 1e-10
+        e = main.entropy_error(ud)[0]
+        om = orc.Mesh.from_export(m.export())
+        d1 = orc.Disc(om, **c["phys"], flux=c["flux"], gradient="NONE", bcs=c["bcs"])
+        d2 = orc.Disc(om, **c["phys"], flux=c["flux"], gradient="GREENGAUSS", bcs=c["bcs"])
+        u1, _ = d1.steady_solve(np.tile(d2.freestream(), (m.nelem, 1)), cflmin=s1["cfl_min"], cflmax=s1["cfl_max"],
+                                tol=s1["tolerance"], maxiter=s1["max_timesteps"], abs_tol=False, pc=c["pc"],
+                                nl_update=c["nl_update"])
+        u2, so = d2.steady_solve(u1, cflmin=s2["cfl_min"], cflmax=s2["cfl_max"], tol=1e-10, maxiter=3000,
+                                 abs_tol=True, pc=c["pc"], nl_update=c["nl_update"])
+        assert so["status"] == 0
+        eo = d2.entropy_error(u2)
+        assert abs(e - eo) <= 1e-8 * eo, (m.nelem, e, eo)
+        logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(e)))
+    slope = (logs[1][1] - logs[0][1]) / (logs[1][0] - logs[0][0])
+    assert 1.65 <= slope <= 2.1, (slope, logs)
