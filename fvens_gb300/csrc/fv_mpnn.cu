@@ -680,15 +680,16 @@ cudaError_t mall(fv_mpnn *N, T **p, size_t n)
 cudaError_t ensure_capacity(fv_mpnn *N, int B)
 {
 	if (B <= N->cap_b) return cudaSuccess;
-	// activations are re-allocated for the larger batch
-	for (void *q : {(void *)N->h, (void *)N->zpre, (void *)N->mpre, (void *)N->agg, (void *)N->upre,
-	                (void *)N->y, (void *)N->dy, (void *)N->cond, (void *)N->uinf, (void *)N->t2, (void *)N->dh,
-	                (void *)N->pc, (void *)N->sgrad, (void *)N->wst, (void *)N->epart, (void *)N->part,
-	                (void *)N->bpart, (void *)N->rtmp, (void *)N->lpart})
-		if (q) {
-			cudaFree(q);
+	// activations are re-allocated for the larger batch; until all of them
+	// are, the network holds none (a failed allocation leaves no stale buffer)
+	N->cap_b = 0;
+	for (float **q : {&N->h, &N->zpre, &N->mpre, &N->agg, &N->upre, &N->y, &N->dy, &N->cond, &N->uinf, &N->t2,
+	                  &N->dh, &N->pc, &N->sgrad, &N->wst, &N->epart, &N->part, &N->bpart, &N->rtmp, &N->lpart})
+		if (*q) {
+			cudaFree(*q);
 			for (auto &o : N->owned)
-				if (o == q) o = nullptr;
+				if (o == *q) o = nullptr;
+			*q = nullptr;
 		}
 	const size_t nc = N->G.nc, nm = 2 * (size_t)N->G.nf, L = N->lay.layers;
 	const size_t rows_m = B * nm, rows_c = B * nc;
