@@ -66,3 +66,10 @@ def load_cylinders():
     z = np.load(os.path.join(GOLDEN, "2dcylinder_meshes.npz"))
     return [fv.UMesh.from_arrays(z[f"m{k}_coords"], z[f"m{k}_nnode"].astype(np.int32), z[f"m{k}_inpoel"],
                                  z[f"m{k}_bface"], z[f"m{k}_btag"].astype(np.int32), reorder=1) for k in range(4)]
+
+
+# The explicit variant (tests/inv-2dcyl/expl-inv-cyl-gg-roe_tri.ctrl, three
+# meshes): Roe, Green-Gauss, forward-Euler starter (CFL 0.5, relative 1e-1,
+# 15000 steps) and main solve (CFL 0.25, relative 1e-4, 60000 steps)
+CYLINDER_EXPLICIT = dict(flux="ROE", gradient="GREENGAUSS", start=dict(cfl=0.5, tolerance=1e-1, max_timesteps=15000),
+                         main=dict(cfl=0.25, tolerance=1e-4, max_timesteps=60000), nmesh=3)

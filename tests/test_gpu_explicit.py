@@ -98,3 +98,37 @@ def test_tvdrk_step_bound(cuda):
     ud = torch.tensor(np.tile(od.freestream(), (m.nelem, 1)), device=cuda)
     rc, steps, tm = gd.tvdrk_solve(ud, 3, 0.2, 1.0e3, max_steps=5, raise_on_error=False)
     assert rc == fv.FV_ERR_TOLERANCE and steps[0] == 5
+
+
+def test_explicit_entropy_convergence_on_reference_cylinders(cuda):
+    """The reference's explicit entropy-convergence test (expl-inv-cyl-gg-roe_tri.ctrl
+    on 2dcylinder1 and 2dcylinder2): the GPU's forward-Euler starter and main
+    solve stop at the oracle's step counts with entropy errors within 1e-8 of
+    the oracle's, and the order between the meshes lies in [1.65, 2.1]."""
+    import torch
+
+    from tests import regression_cases as rcases
+    c, x = rcases.CYLINDER, rcases.CYLINDER_EXPLICIT
+    s1, s2 = x["start"], x["main"]
+    logs = []
+    for m in rcases.load_cylinders()[1:3]:
+        ph = fv.physics_cfg(**c["phys"])
+        start = fv.FlowFV(m, ph, fv.numerics_cfg(flux=x["flux"], gradient="NONE"), c["bcs"])
+        main = fv.FlowFV(m, ph, fv.numerics_cfg(flux=x["flux"], gradient=x["gradient"]), c["bcs"])
+        ud = torch.tensor(np.tile(main.freestream()[0], (m.nelem, 1)), device=cuda)
+        _, st1 = start.steady_fe_solve(ud, cfl=s1["cfl"], tolerance=s1["tolerance"],
+                                       max_timesteps=s1["max_timesteps"], abs_tolerance=False)
+        _, st2 = main.steady_fe_solve(ud, cfl=s2["cfl"], tolerance=s2["tolerance"],
+                                      max_timesteps=s2["max_timesteps"], abs_tolerance=False)
+        om = orc.Mesh.from_export(m.export())
+        d1 = orc.Disc(om, **c["phys"], flux=x["flux"], gradient="NONE", bcs=c["bcs"])
+        d2 = orc.Disc(om, **c["phys"], flux=x["flux"], gradient=x["gradient"], bcs=c["bcs"])
+        u1, a = d1.steady_fe(np.tile(d2.freestream(), (m.nelem, 1)), s1["cfl"], tol=s1["tolerance"],
+                             maxiter=s1["max_timesteps"], abs_tol=False)
+        u2, b = d2.steady_fe(u1, s2["cfl"], tol=s2["tolerance"], maxiter=s2["max_timesteps"], abs_tol=False)
+        assert (st1[0]["steps"], st2[0]["steps"]) == (a["steps"], b["steps"])
+        e, eo = main.entropy_error(ud)[0], d2.entropy_error(u2)
+        assert abs(e - eo) <= 1e-8 * eo, (m.nelem, e, eo)
+        logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(e)))
+    slope = (logs[1][1] - logs[0][1]) / (logs[1][0] - logs[0][0])
+    assert 1.65 <= slope <= 2.1, (slope, logs)

@@ -75,3 +75,24 @@ def test_oracle_entropy_convergence_on_reference_cylinders(gradient):
     assert all(s in (0, 6) for s in statuses[2:]), statuses
     slope = (logs[3][1] - logs[2][1]) / (logs[3][0] - logs[2][0])
     assert 1.65 <= slope <= 2.1, (slope, logs, statuses)
+
+
+def test_oracle_explicit_entropy_convergence_on_reference_cylinders():
+    """The reference's Flow_Explicit_Euler_Cylinder_GreenGauss_Roe_Tri_EntropyConvergence
+    (tests/flow_conv.cpp with expl-inv-cyl-gg-roe_tri.ctrl, 2dcylinder0..2):
+    forward-Euler starter and main solve from freestream; the last order lies
+    in [1.65, 2.1].  The oracle's solves all reach their relative tolerance."""
+    c, x = rc.CYLINDER, rc.CYLINDER_EXPLICIT
+    logs = []
+    for m in rc.load_cylinders()[:x["nmesh"]]:
+        om = orc.Mesh.from_export(m.export())
+        d1 = orc.Disc(om, **c["phys"], flux=x["flux"], gradient="NONE", bcs=c["bcs"])
+        d2 = orc.Disc(om, **c["phys"], flux=x["flux"], gradient=x["gradient"], bcs=c["bcs"])
+        s1, s2 = x["start"], x["main"]
+        u1, a = d1.steady_fe(np.tile(d2.freestream(), (m.nelem, 1)), s1["cfl"], tol=s1["tolerance"],
+                             maxiter=s1["max_timesteps"], abs_tol=False)
+        u2, b = d2.steady_fe(u1, s2["cfl"], tol=s2["tolerance"], maxiter=s2["max_timesteps"], abs_tol=False)
+        assert a["status"] == 0 and b["status"] == 0, (m.nelem, a["status"], b["status"])
+        logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(d2.entropy_error(u2))))
+    slope = (logs[-1][1] - logs[-2][1]) / (logs[-1][0] - logs[-2][0])
+    assert 1.65 <= slope <= 2.1, (slope, logs)
