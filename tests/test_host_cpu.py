@@ -95,6 +95,37 @@ def test_gmsh_reader_on_reference_meshes(name):
     _compare_topology(m)
 
 
+def _cell_edges(e, c):
+    k = int(e["nnode"][c])
+    nodes = e["inpoel"][c, :k]
+    return {frozenset((int(nodes[j]), int(nodes[(j + 1) % k]))) for j in range(k)}
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference test meshes not present")
+@pytest.mark.parametrize("name", ["2dcylinderhybrid.msh", "testhybrid.msh"])
+def test_faces_belong_to_their_cells(name):
+    """The reference's Mesh_Topology_FaceStructure / ElemSurrElem consistency
+    checks (tests/mesh/mesh.cpp:14-64): every boundary face is an edge of its
+    cell; every interior face is an edge shared by its two cells, and its unit
+    normal is perpendicular to that edge, with the edge's length, pointing
+    from the left cell to the right one."""
+    m = fv.UMesh.read_gmsh(os.path.join(REF_MESHES, name))
+    e, g = m.export(), m.geometry()
+    xy, lr, fn = e["coords"], g["face_lr"], g["fnorm"]
+    for f in range(m.nbface):
+        assert frozenset(int(x) for x in e["bface"][f]) in _cell_edges(e, lr[f, 0])
+    for f in range(m.nbface, m.naface):
+        L, R = lr[f]
+        assert 0 <= L < R < m.nelem
+        shared = _cell_edges(e, L) & _cell_edges(e, R)
+        assert len(shared) == 1
+        a, b = sorted(next(iter(shared)))
+        d = xy[b] - xy[a]
+        assert abs(fn[f, 0] * d[0] + fn[f, 1] * d[1]) <= 1e-12 * fn[f, 2]
+        assert abs(np.hypot(*d) - fn[f, 2]) <= 1e-12 * fn[f, 2]
+        assert fn[f, 0] * (g["cc"][R, 0] - g["cc"][L, 0]) + fn[f, 1] * (g["cc"][R, 1] - g["cc"][L, 1]) > 0
+
+
 REF_TESTCASES = os.path.join(os.path.dirname(REF_MESHES), "..", "testcases") if REF_MESHES else ""
 
 
