@@ -1,8 +1,8 @@
 """The multi-rank (replica) path on CPU with gloo, world size 2: each rank
 solves its own flow condition (with the oracle standing in for the GPU
 solve), the timing is the maximum over ranks and the throughput counts every
-rank's solves; and bench.py's reference arm under torchrun prints one line
-from rank 0 only."""
+rank's solves; bench.py's reference arm under torchrun prints one line
+from rank 0 only; and bench.py's CPU-baseline leg runs on a small mesh."""
 import json
 import os
 import socket
@@ -79,3 +79,20 @@ def test_reference_arm_under_torchrun_prints_once():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0 and line["n_gpus"] == 2
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_bench_cpu_baseline_on_small_naca_mesh():
+    """bench.py's CPU-baseline leg (the oracle's step model and its kernel
+    timings) on a small O-grid of the workload's family: a positive solve rate
+    in the metric's unit, the sample described, and every kernel timed."""
+    sys.path.insert(0, ROOT)
+    import bench
+    import fvens_gb300 as fv
+    m = fv.UMesh.generate(fv.MESH_NACA_OGRID, [64, 32, 30.0, 0, 0, 1.1, 12, 3], reorder=1)
+    _, od2 = bench._oracle_case(m)
+    u = np.tile(od2.freestream(), (m.nelem, 1))
+    cb = bench.cpu_baseline(m, {"steps": 10, "lin_iters": 50}, {"steps": 20, "lin_iters": 200}, 1.0, u)
+    assert cb["unit"] == "solves/s" and cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1
+    assert "10 + 20 steps" in cb["sample"]
+    assert set(cb["kernels_ms"]) == {"residual", "jacobian", "ilu0_setup", "ilu0_apply"}
+    assert all(v > 0 for v in cb["kernels_ms"].values())
