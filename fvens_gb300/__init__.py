@@ -158,6 +158,14 @@ class UMesh:
         check(lib().fv_mesh_find_lines(self._h, ctypes.c_double(threshold), ctypes.byref(nl), _hp(cl, ctypes.c_int)))
         return nl.value, cl
 
+    def line_ordering(self):
+        """The reference's hybrid line ordering with the natural graph order:
+        the cells of each line found by find_lines, then the other cells;
+        returns the cell at each position."""
+        order = np.zeros(self.nelem, np.int32)
+        check(lib().fv_mesh_line_ordering(self._h, _hp(order, ctypes.c_int)))
+        return order
+
     def export(self):
         coords = np.zeros((self.npoin, 2))
         nnode = np.zeros(self.nelem, np.int32)

@@ -232,6 +232,19 @@ fv_status fv_mesh_find_lines(fv_mesh *m, double threshold, int *nlines, int *cel
 	return FV_OK;
 }
 
+fv_status fv_mesh_line_ordering(const fv_mesh *m, int *order)
+{
+	if (!m || !order) { set_error("null argument"); return FV_ERR_INVALID; }
+	const HostMesh &h = m->h;
+	int k = 0;
+	for (const std::vector<int> &ln : h.lines)
+		for (int c : ln) order[k++] = c;
+	for (int c = 0; c < h.nelem; c++)
+		if (h.cell_line.empty() || h.cell_line[c] < 0) order[k++] = c;
+	if (k != h.nelem) { set_error("inconsistent lines"); return FV_ERR_MESH; }
+	return FV_OK;
+}
+
 fv_status fv_mesh_periodic_map(const fv_mesh *m, int marker, int axis, int *map)
 {
 	if (!m || !map) { set_error("null argument"); return FV_ERR_INVALID; }

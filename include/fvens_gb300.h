@@ -130,6 +130,11 @@ fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *
  * parts.  threshold <= 0 removes them.  *nlines, cell_line[nelem] (line index
  * or -1; either may be NULL) receive the result. */
 fv_status fv_mesh_find_lines(fv_mesh *m, double threshold, int *nlines, int *cell_line);
+/* getHybridLineOrdering with the "natural" graph ordering (meshordering.cpp:69-141):
+ * the cells of each line found by fv_mesh_find_lines, line by line in line
+ * order, then the cells outside lines in index order; order[nelem] = cell at
+ * each position (the identity when no lines were found). */
+fv_status fv_mesh_line_ordering(const fv_mesh *m, int *order);
 /* UMesh::compute_periodic_map (mesh.cpp:368-421): pairs the boundary faces of
  * `marker` whose centres agree (to 1e-8) along the axis other than `axis`
  * (0 = x, 1 = y); map[nbface] = partner boundary face or -1.  The flow

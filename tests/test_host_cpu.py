@@ -404,3 +404,17 @@ def test_find_lines_matches_reference_golden_lines():
     for k, cells in enumerate(gold):
         assert [int(cl[c]) for c in cells] == [k] * len(cells)
     assert int((cl >= 0).sum()) == sum(len(g) for g in gold)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference test meshes not present")
+def test_line_ordering_matches_reference_golden_ordering():
+    """tests/mesh/testhybridlineordering.cpp (MeshUtils_hybridLineOrdering_natural_smallmesh):
+    on testanisotropic.msh with threshold 10 the natural hybrid line ordering
+    is testanisotropic-lineordering.txt (Gmsh element numbers, boundary
+    elements first).  Without lines the ordering is the identity."""
+    m = fv.UMesh.read_gmsh(os.path.join(REF_MESHES, "testanisotropic.msh"), reorder=0)
+    assert np.array_equal(m.line_ordering(), np.arange(m.nelem))
+    m.find_lines(10.0)
+    with open(os.path.join(REF_MESHES, "testanisotropic-lineordering.txt")) as f:
+        gold = [int(c) - m.nbface - 1 for c in f.read().split()]
+    assert m.line_ordering().tolist() == gold
