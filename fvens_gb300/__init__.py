@@ -158,12 +158,12 @@ class UMesh:
         check(lib().fv_mesh_find_lines(self._h, ctypes.c_double(threshold), ctypes.byref(nl), _hp(cl, ctypes.c_int)))
         return nl.value, cl
 
-    def line_ordering(self):
-        """The reference's hybrid line ordering with the natural graph order:
-        the cells of each line found by find_lines, then the other cells;
-        returns the cell at each position."""
+    def line_ordering(self, rcm=False):
+        """The reference's hybrid line ordering on the lines found by
+        find_lines, with the natural or the RCM order of the graph of lines
+        and remaining cells; returns the cell at each position."""
         order = np.zeros(self.nelem, np.int32)
-        check(lib().fv_mesh_line_ordering(self._h, _hp(order, ctypes.c_int)))
+        check(lib().fv_mesh_line_ordering(self._h, int(bool(rcm)), _hp(order, ctypes.c_int)))
         return order
 
     def export(self):

@@ -232,15 +232,120 @@ fv_status fv_mesh_find_lines(fv_mesh *m, double threshold, int *nlines, int *cel
 	return FV_OK;
 }
 
-fv_status fv_mesh_line_ordering(const fv_mesh *m, int *order)
+}  // extern "C"
+
+namespace {
+
+/* SPARSEPACK GENRCM (A. George and J. W. Liu, Computer Solution of Large
+ * Sparse Positive Definite Systems, 1981), the ordering behind PETSc's
+ * MatGetOrdering "rcm": per connected component, in order of the lowest
+ * unnumbered vertex, a pseudo-peripheral root (FNROOT: restart from a vertex
+ * of minimum degree in the last level while the level structure deepens),
+ * then breadth-first numbering with each vertex's new neighbours in
+ * increasing degree (stable), reversed.  adj: sorted neighbour lists without
+ * the vertex itself.  Returns the vertex at each position. */
+std::vector<int> genrcm(const std::vector<std::vector<int>> &adj)
+{
+	const int n = (int)adj.size();
+	std::vector<char> mask(n, 1), seen(n, 0);
+	std::vector<int> out, deg(n), ls, lp;
+	out.reserve(n);
+	auto rootls = [&](int root) {  // level structure of root's unnumbered component
+		ls.assign(1, root);
+		lp.assign(1, 0);
+		seen[root] = 1;
+		size_t b = 0;
+		while (true) {
+			const size_t e = ls.size();
+			for (size_t i = b; i < e; i++)
+				for (int x : adj[ls[i]])
+					if (mask[x] && !seen[x]) { seen[x] = 1; ls.push_back(x); }
+			if (ls.size() == e) break;
+			lp.push_back((int)e);
+			b = e;
+		}
+		for (int x : ls) seen[x] = 0;
+	};
+	auto degree = [&](int v) { int d = 0; for (int x : adj[v]) d += mask[x]; return d; };
+	for (int s = 0; s < n; s++) {
+		if (!mask[s]) continue;
+		int root = s;
+		rootls(root);
+		int nlvl = (int)lp.size();
+		const int ccsize = (int)ls.size();
+		while (nlvl > 1 && nlvl < ccsize) {
+			const int j0 = lp.back();
+			int mindeg = ccsize;
+			root = ls[j0];
+			if (ccsize - j0 > 1)
+				for (int j = j0; j < ccsize; j++) {
+					const int d = degree(ls[j]);
+					if (d < mindeg) { root = ls[j]; mindeg = d; }
+				}
+			rootls(root);
+			if ((int)lp.size() <= nlvl) break;
+			nlvl = (int)lp.size();
+		}
+		for (int x : ls) deg[x] = degree(x);
+		const size_t c0 = out.size();
+		out.push_back(root);
+		mask[root] = 0;
+		for (size_t i = c0; i < out.size(); i++) {
+			const size_t f = out.size();
+			for (int x : adj[out[i]])
+				if (mask[x]) { mask[x] = 0; out.push_back(x); }
+			std::stable_sort(out.begin() + f, out.end(), [&](int a, int b) { return deg[a] < deg[b]; });
+		}
+		std::reverse(out.begin() + c0, out.end());
+	}
+	return out;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* getHybridLineOrdering (meshordering.cpp:69-141, 267-402): a graph whose
+ * vertices are the lines, then the cells outside lines; two vertices are
+ * adjacent when a cell of one shares a face with a cell of the other.  The
+ * graph is taken in natural order or reordered by RCM, and each line vertex
+ * expands to its cells in line order. */
+fv_status fv_mesh_line_ordering(const fv_mesh *m, int rcm, int *order)
 {
 	if (!m || !order) { set_error("null argument"); return FV_ERR_INVALID; }
 	const HostMesh &h = m->h;
+	const int nl = (int)h.lines.size();
+	std::vector<int> points, vid(h.nelem);
+	for (int c = 0; c < h.nelem; c++) {
+		if (!h.cell_line.empty() && h.cell_line[c] >= 0) {
+			vid[c] = h.cell_line[c];
+		} else {
+			vid[c] = nl + (int)points.size();
+			points.push_back(c);
+		}
+	}
+	const int nv = nl + (int)points.size();
+	std::vector<int> gorder(nv);
+	for (int v = 0; v < nv; v++) gorder[v] = v;
+	if (rcm) {
+		std::vector<std::vector<int>> adj(nv);
+		for (int f = h.nbface; f < h.naface; f++) {
+			const int a = vid[h.face_l[f]], b = vid[h.face_r[f]];
+			if (a != b) { adj[a].push_back(b); adj[b].push_back(a); }
+		}
+		for (std::vector<int> &a : adj) {
+			std::sort(a.begin(), a.end());
+			a.erase(std::unique(a.begin(), a.end()), a.end());
+		}
+		gorder = genrcm(adj);
+	}
 	int k = 0;
-	for (const std::vector<int> &ln : h.lines)
-		for (int c : ln) order[k++] = c;
-	for (int c = 0; c < h.nelem; c++)
-		if (h.cell_line.empty() || h.cell_line[c] < 0) order[k++] = c;
+	for (int v : gorder) {
+		if (v < nl)
+			for (int c : h.lines[v]) order[k++] = c;
+		else
+			order[k++] = points[v - nl];
+	}
 	if (k != h.nelem) { set_error("inconsistent lines"); return FV_ERR_MESH; }
 	return FV_OK;
 }

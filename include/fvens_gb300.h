@@ -130,11 +130,13 @@ fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *
  * parts.  threshold <= 0 removes them.  *nlines, cell_line[nelem] (line index
  * or -1; either may be NULL) receive the result. */
 fv_status fv_mesh_find_lines(fv_mesh *m, double threshold, int *nlines, int *cell_line);
-/* getHybridLineOrdering with the "natural" graph ordering (meshordering.cpp:69-141):
- * the cells of each line found by fv_mesh_find_lines, line by line in line
- * order, then the cells outside lines in index order; order[nelem] = cell at
- * each position (the identity when no lines were found). */
-fv_status fv_mesh_line_ordering(const fv_mesh *m, int *order);
+/* getHybridLineOrdering (meshordering.cpp:69-141) on the lines found by
+ * fv_mesh_find_lines: rcm = 0 ("natural") gives the cells of each line, line
+ * by line, then the cells outside lines in index order; rcm = 1 first
+ * reorders the graph of lines and remaining cells by reverse Cuthill-McKee
+ * (PETSc's "rcm", SPARSEPACK GENRCM).  order[nelem] = cell at each position
+ * (without lines: the identity, or the RCM order of the cells). */
+fv_status fv_mesh_line_ordering(const fv_mesh *m, int rcm, int *order);
 /* UMesh::compute_periodic_map (mesh.cpp:368-421): pairs the boundary faces of
  * `marker` whose centres agree (to 1e-8) along the axis other than `axis`
  * (0 = x, 1 = y); map[nbface] = partner boundary face or -1.  The flow

@@ -408,13 +408,21 @@ def test_find_lines_matches_reference_golden_lines():
 
 @pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference test meshes not present")
 def test_line_ordering_matches_reference_golden_ordering():
-    """tests/mesh/testhybridlineordering.cpp (MeshUtils_hybridLineOrdering_natural_smallmesh):
-    on testanisotropic.msh with threshold 10 the natural hybrid line ordering
-    is testanisotropic-lineordering.txt (Gmsh element numbers, boundary
-    elements first).  Without lines the ordering is the identity."""
+    """tests/mesh/testhybridlineordering.cpp (MeshUtils_hybridLineOrdering_{natural,rcm}_smallmesh):
+    on testanisotropic.msh with threshold 10 the hybrid line orderings are
+    testanisotropic-lineordering.txt and testanisotropic-line_rcm_ordering.txt
+    (Gmsh element numbers, boundary elements first).  Without lines the
+    natural ordering is the identity."""
     m = fv.UMesh.read_gmsh(os.path.join(REF_MESHES, "testanisotropic.msh"), reorder=0)
     assert np.array_equal(m.line_ordering(), np.arange(m.nelem))
     m.find_lines(10.0)
-    with open(os.path.join(REF_MESHES, "testanisotropic-lineordering.txt")) as f:
-        gold = [int(c) - m.nbface - 1 for c in f.read().split()]
-    assert m.line_ordering().tolist() == gold
+    for rcm, name in ((False, "testanisotropic-lineordering.txt"), (True, "testanisotropic-line_rcm_ordering.txt")):
+        with open(os.path.join(REF_MESHES, name)) as f:
+            gold = [int(c) - m.nbface - 1 for c in f.read().split()]
+        assert m.line_ordering(rcm).tolist() == gold, name
+    # a boundary-layer O-grid, with and without lines: permutations of its cells
+    big = cases.naca_visc()
+    for thr in (0.0, 10.0):
+        big.find_lines(thr)
+        for rcm in (False, True):
+            assert np.array_equal(np.sort(big.line_ordering(rcm)), np.arange(big.nelem))
