@@ -58,6 +58,7 @@ class fv_bc_cfg(ctypes.Structure):
 
 
 _lib = None
+ABI_VERSION = 2  # FVENS_GB300_ABI_VERSION of include/fvens_gb300.h
 
 
 def lib():
@@ -77,6 +78,10 @@ def lib():
         L.fv_precond_destroy.restype = None
         L.fv_solver_destroy.restype = None
         L.fv_solver_cfg_default.restype = None
+        ver = L.fv_abi_version() if hasattr(L, "fv_abi_version") else 1
+        if ver != ABI_VERSION:
+            raise RuntimeError(f"{LIB_PATH} has ABI version {ver}, this binding expects "
+                               f"{ABI_VERSION}; rebuild with `python -m fvens_gb300.build`")
         _lib = L
     return _lib
 

@@ -94,15 +94,16 @@ def build_oracle():
     return ORACLE_LIB
 
 
-def build_reference_shim(reference_root="/root/reference"):
+def build_reference_shim(reference_root=None):
     """Compiles the reference's own pointwise physics into oracle/_ref (only
-    where the reference sources exist)."""
-    if not os.path.isdir(os.path.join(reference_root, "src")):
-        return None
+    where the reference sources exist).  reference_root: the reference
+    project's root; by default oracle/ref/build_ref.sh picks it
+    ($FVENS_REFERENCE or its own default) and skips when it is absent."""
     shim = os.path.join(ORACLE_DIR, "ref", "ref_wrap.cpp")
-    if _stale(REF_LIB, [shim]):
-        _run(["sh", os.path.join(ORACLE_DIR, "ref", "build_ref.sh"), reference_root])
-    return REF_LIB
+    recipe = os.path.join(ORACLE_DIR, "ref", "build_ref.sh")
+    if _stale(REF_LIB, [shim, recipe]):
+        _run(["sh", recipe] + ([reference_root] if reference_root else []))
+    return REF_LIB if os.path.exists(REF_LIB) else None
 
 
 def build_all(verbose=False):

@@ -119,6 +119,8 @@ Phys make_phys(const fv_physics_cfg &c)
 
 extern "C" {
 
+int fv_abi_version(void) { return FVENS_GB300_ABI_VERSION; }
+
 const char *fv_status_string(fv_status s)
 {
 	switch (s) {
@@ -416,6 +418,7 @@ fv_status fv_disc_create(fv_mesh *m, const fv_physics_cfg *phys, int batch, cons
 	fv_disc *D = new fv_disc();
 	D->mesh = m;
 	D->batch = batch;
+	cudaGetDevice(&D->device);
 	// BC table (create_const_flowBCs, abc.cpp:460-500)
 	std::map<int, int> tag2idx;
 	for (int k = 0; k < nbc; k++) {

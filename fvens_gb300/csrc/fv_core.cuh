@@ -111,18 +111,20 @@ struct fv_disc_impl {
 	int *btag = nullptr;       // device: boundary marker of each boundary face
 	double *surf = nullptr;    // device: surface-integral partials [batch][4]
 	cudaStream_t stream = 0;
+	int device = 0;            // CUDA device current when the handle was created
 	int kernels_launched = 0;  // running count of this handle's kernel launches
 };
 
 // ------------------------------- kernels -------------------------------------
+/* w: the scratch to evaluate into (NULL: the handle's own, D->w) */
 cudaError_t residual_launch(fv_disc_impl *D, const double *u, double *r, int gettimesteps, double *dt,
-                            cudaStream_t s);
+                            cudaStream_t s, const ResidualWork *w = nullptr);
 cudaError_t gradients_launch(fv_disc_impl *D, const double *u, double *grad, int conserved, cudaStream_t s);
 /* the residual's passes before the face kernel (primitive/ghost states,
  * gradients, limiter values, WENO blend) into the handle's scratch */
 /* the passes before the face kernel; with x, at the state u + pm x (per member pm) */
 cudaError_t gradient_pass_launch(fv_disc_impl *D, const double *u, cudaStream_t s, const double *x = nullptr,
-                                 const double *pm = nullptr);
+                                 const double *pm = nullptr, const ResidualWork *w = nullptr);
 cudaError_t residual_mf_launch(fv_disc_impl *D, const double *u, const double *up, const double *x, const double *r,
                                const double *dtm, const double *pm, double *y, cudaStream_t s);
 /* times the residual kernels at 64 / 128 / 256 threads per block at state u
@@ -130,7 +132,8 @@ cudaError_t residual_mf_launch(fv_disc_impl *D, const double *u, const double *u
 cudaError_t residual_autotune(fv_disc_impl *D, const double *u, cudaStream_t s, int *chosen);
 /* the face-flux launch alone (reads the prep/gradient/limiter results of the
  * last residual evaluation of the same state) */
-cudaError_t face_launch(fv_disc_impl *D, const double *u, int gettimesteps, cudaStream_t s);
+cudaError_t face_launch(fv_disc_impl *D, const double *u, int gettimesteps, cudaStream_t s,
+                        const ResidualWork *w = nullptr);
 
 /* Block-row matrix: 5 slots per cell (0 = diagonal, 1+j = neighbour across
  * local edge j); values [batch][slot][cell][16], FP32 or FP64. */

@@ -137,13 +137,14 @@ __global__ void __launch_bounds__(kMaxBS) k_gather_mf(DiscDev D, ResidualWork w,
 }
 
 template <int FLUX>
-void launch_face(fv_disc_impl *Dh, const double *u, int getdt, dim3 grid, int bs, cudaStream_t s)
+void launch_face(fv_disc_impl *Dh, const ResidualWork &W, const double *u, int getdt, dim3 grid, int bs,
+                 cudaStream_t s)
 {
 	const DiscDev &D = Dh->d;
 	const int visc = !D.viscous ? 0 : (D.constvisc ? 2 : 1);
-	if (visc == 0) k_face<FLUX, 0><<<grid, bs, 0, s>>>(D, u, Dh->w, getdt);
-	else if (visc == 1) k_face<FLUX, 1><<<grid, bs, 0, s>>>(D, u, Dh->w, getdt);
-	else k_face<FLUX, 2><<<grid, bs, 0, s>>>(D, u, Dh->w, getdt);
+	if (visc == 0) k_face<FLUX, 0><<<grid, bs, 0, s>>>(D, u, W, getdt);
+	else if (visc == 1) k_face<FLUX, 1><<<grid, bs, 0, s>>>(D, u, W, getdt);
+	else k_face<FLUX, 2><<<grid, bs, 0, s>>>(D, u, W, getdt);
 }
 
 /* grid of n items in blocks of bs, one row per batch member */
@@ -151,19 +152,20 @@ dim3 grid_of(int n, int bs, int batch) { return dim3((unsigned)((n + bs - 1) / b
 
 }  // namespace
 
-cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cudaStream_t s)
+cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cudaStream_t s, const ResidualWork *w)
 {
 	const DiscDev &D = Dh->d;
+	const ResidualWork &W = w ? *w : Dh->w;
 	const int bs = Dh->bs[KBS_FACE];
 	const dim3 gf = grid_of(D.naface, bs, Dh->batch);
 	switch (D.flux) {
-	case FLUX_LLF: launch_face<FLUX_LLF>(Dh, u, gettimesteps, gf, bs, s); break;
-	case FLUX_VANLEER: launch_face<FLUX_VANLEER>(Dh, u, gettimesteps, gf, bs, s); break;
-	case FLUX_AUSM: launch_face<FLUX_AUSM>(Dh, u, gettimesteps, gf, bs, s); break;
-	case FLUX_AUSMPLUS: launch_face<FLUX_AUSMPLUS>(Dh, u, gettimesteps, gf, bs, s); break;
-	case FLUX_ROE: launch_face<FLUX_ROE>(Dh, u, gettimesteps, gf, bs, s); break;
-	case FLUX_HLL: launch_face<FLUX_HLL>(Dh, u, gettimesteps, gf, bs, s); break;
-	default: launch_face<FLUX_HLLC>(Dh, u, gettimesteps, gf, bs, s); break;
+	case FLUX_LLF: launch_face<FLUX_LLF>(Dh, W, u, gettimesteps, gf, bs, s); break;
+	case FLUX_VANLEER: launch_face<FLUX_VANLEER>(Dh, W, u, gettimesteps, gf, bs, s); break;
+	case FLUX_AUSM: launch_face<FLUX_AUSM>(Dh, W, u, gettimesteps, gf, bs, s); break;
+	case FLUX_AUSMPLUS: launch_face<FLUX_AUSMPLUS>(Dh, W, u, gettimesteps, gf, bs, s); break;
+	case FLUX_ROE: launch_face<FLUX_ROE>(Dh, W, u, gettimesteps, gf, bs, s); break;
+	case FLUX_HLL: launch_face<FLUX_HLL>(Dh, W, u, gettimesteps, gf, bs, s); break;
+	default: launch_face<FLUX_HLLC>(Dh, W, u, gettimesteps, gf, bs, s); break;
 	}
 	return cudaGetLastError();
 }
@@ -171,29 +173,30 @@ cudaError_t face_launch(fv_disc_impl *Dh, const double *u, int gettimesteps, cud
 /* the residual's passes before the face kernel: primitive and ghost states,
  * gradients (+ Barth-Jespersen / Venkatakrishnan limiter values), WENO blend */
 cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t s, const double *x,
-                                 const double *pm)
+                                 const double *pm, const ResidualWork *w)
 {
 	const DiscDev &D = Dh->d;
+	const ResidualWork &W = w ? *w : Dh->w;
 	const int B = Dh->batch;
 	const int bp = Dh->bs[KBS_PREP], bg = Dh->bs[KBS_GRAD];
 	int nk = 0;
-	if (x) k_prep_mf<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, x, pm, Dh->w);
-	else k_prep<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, Dh->w);
+	if (x) k_prep_mf<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, x, pm, W);
+	else k_prep<<<grid_of(D.nelem + D.nbface, bp, B), bp, 0, s>>>(D, u, W);
 	nk++;
 	if (D.gradscheme != GRAD_NONE) {
 		const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
-		k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, lim);
+		k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.prim, W.ghost_prim, W.grad, W.phi, lim);
 		nk++;
 		if (D.recon == REC_WENO) {
-			k_weno<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, Dh->w.grad, Dh->w.lgrad);
+			k_weno<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.grad, W.lgrad);
 			nk++;
 		}
 	} else {
-		cudaMemsetAsync(Dh->w.grad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
-		if (D.recon == REC_WENO) cudaMemsetAsync(Dh->w.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
+		cudaMemsetAsync(W.grad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
+		if (D.recon == REC_WENO) cudaMemsetAsync(W.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
 		if (D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN) {
 			// zero gradients: every face value equals the cell value, the limiter is 1
-			k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad, Dh->w.phi, 0);
+			k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.prim, W.ghost_prim, W.grad, W.phi, 0);
 			nk++;
 		}
 	}
@@ -201,16 +204,18 @@ cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t
 	return cudaGetLastError();
 }
 
-cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int gettimesteps, double *dt, cudaStream_t s)
+cudaError_t residual_launch(fv_disc_impl *Dh, const double *u, double *r, int gettimesteps, double *dt, cudaStream_t s,
+                            const ResidualWork *w)
 {
 	const DiscDev &D = Dh->d;
+	const ResidualWork &W = w ? *w : Dh->w;
 	if (D.order2) {
-		const cudaError_t e = gradient_pass_launch(Dh, u, s);
+		const cudaError_t e = gradient_pass_launch(Dh, u, s, nullptr, nullptr, &W);
 		if (e) return e;
 	}
-	face_launch(Dh, u, gettimesteps, s);
+	face_launch(Dh, u, gettimesteps, s, &W);
 	const int bc = Dh->bs[KBS_GATHER];
-	k_gather<<<grid_of(D.nelem, bc, Dh->batch), bc, 0, s>>>(D, Dh->w, r, gettimesteps ? dt : nullptr);
+	k_gather<<<grid_of(D.nelem, bc, Dh->batch), bc, 0, s>>>(D, W, r, gettimesteps ? dt : nullptr);
 	Dh->kernels_launched += 2;
 	return cudaGetLastError();
 }

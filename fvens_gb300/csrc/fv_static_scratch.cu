@@ -15,7 +15,10 @@
  *
  * Set-up: the first call on a device, with that device current, looks up the
  * array's device address with cudaGetSymbolAddress (once per device; the
- * result is kept).  Make that first call before any stream capture.
+ * result is kept).  Make that first call before any stream capture.  The
+ * device current at the call must be the one the handle was created on
+ * (FV_ERR_INVALID otherwise).  The handle itself is only read: its own
+ * scratch buffers stay untouched.
  *
  * Limit: the scratch of one evaluation must fit in kStaticScratchBytes
  * (64 MiB): larger discretisations (cells x batch) are rejected with
@@ -85,6 +88,11 @@ extern "C" fv_status fv_compute_residual_static(fv_disc *D, const double *u, dou
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if (e) return cuda_status(e, "static residual scratch: current device");
+	if (dev != D->device) {
+		set_error("static residual scratch: the handle was created on device " + std::to_string(D->device) +
+		          " but device " + std::to_string(dev) + " is current");
+		return FV_ERR_INVALID;
+	}
 	void *base = nullptr;
 	{
 		std::lock_guard<std::mutex> lk(g_mu);
@@ -98,11 +106,8 @@ extern "C" fv_status fv_compute_residual_static(fv_disc *D, const double *u, dou
 	}
 	ResidualWork w;
 	carve(D->d, D->batch, weno, static_cast<unsigned char *>(base), &w);
-	const ResidualWork own = D->w;
-	D->w = w;
 	const int before = D->kernels_launched;
-	e = residual_launch(D, u, r, gettimesteps, dt, D->stream);
+	e = residual_launch(D, u, r, gettimesteps, dt, D->stream, &w);
 	count_launches(D->kernels_launched - before);
-	D->w = own;
 	return cuda_status(e, "residual (static scratch)");
 }

@@ -35,6 +35,12 @@
 extern "C" {
 #endif
 
+/* ABI version of this header.  A caller compiled against it checks
+ * fv_abi_version() == FVENS_GB300_ABI_VERSION after loading the library.
+ *   1  first release
+ *   2  fv_mesh_line_ordering gained its `rcm` argument (before `order`) */
+#define FVENS_GB300_ABI_VERSION 2
+
 typedef int fv_status;
 #define FV_OK 0
 #define FV_ERR_INVALID 1      /* bad argument or configuration */
@@ -43,6 +49,9 @@ typedef int fv_status;
 #define FV_ERR_TOLERANCE 4    /* max steps reached (reference: Tolerance_error) */
 #define FV_ERR_UNSUPPORTED 5  /* option the reference does not implement (e.g. VanLeer Jacobian) */
 #define FV_ERR_MESH 6         /* mesh topology/geometry error */
+
+/* FVENS_GB300_ABI_VERSION of the loaded library */
+int fv_abi_version(void);
 
 /* inviscid fluxes (afactory.cpp:31-92 names) */
 #define FV_FLUX_LLF 0
@@ -185,7 +194,8 @@ fv_status fv_compute_residual(fv_disc *d, const double *d_u, double *d_r, int ge
  * reference.  For callers whose evaluation path must not allocate device
  * memory: neither the call nor its set-up allocates.  The first call on a
  * device (that device current) looks up the array's address -- make it
- * before any stream capture.  Discretisations whose scratch (cells x batch)
+ * before any stream capture.  The handle's device must be current
+ * (FV_ERR_INVALID otherwise).  Discretisations whose scratch (cells x batch)
  * exceeds the array are rejected with FV_ERR_INVALID.  All calls share the
  * array: calls whose GPU work overlaps race on it. */
 fv_status fv_compute_residual_static(fv_disc *d, const double *d_u, double *d_r, int gettimesteps, double *d_dt);

@@ -52,6 +52,19 @@ def ref_lib():
     return _ref
 
 
+def reference_root():
+    """Root of the reference project's sources, for tests and fixture scripts
+    that read its own inputs: $FVENS_REFERENCE, else the root recorded by
+    oracle/ref/build_ref.sh when it found the sources; None when neither names
+    an existing directory."""
+    cand = os.environ.get("FVENS_REFERENCE")
+    if not cand:
+        rec = os.path.join(_HERE, "_ref", "reference_root.txt")
+        if os.path.exists(rec):
+            cand = open(rec).read().strip()
+    return cand if cand and os.path.isdir(cand) else None
+
+
 def set_threads(n):
     lib().orc_set_threads(int(n))
 

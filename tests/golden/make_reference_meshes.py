@@ -1,7 +1,7 @@
 """Writes the reference's regression meshes as compact arrays for the tests
 (the reference tree is not available where the GPU tests run).
 
-    python tests/golden/make_reference_meshes.py [REFERENCE_ROOT]
+    python tests/golden/make_reference_meshes.py [REFERENCE_ROOT]   (default: $FVENS_REFERENCE)
 
 Reads, with this project's own Gmsh 2.2 reader (cells kept in file order):
   testcases/naca0012/grids/naca0012luo.msh                 -> naca0012luo_mesh.npz
@@ -55,4 +55,8 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    from oracle import orc
+    root = sys.argv[1] if len(sys.argv) > 1 else orc.reference_root()
+    if not root:
+        sys.exit("usage: make_reference_meshes.py REFERENCE_ROOT (or set FVENS_REFERENCE)")
+    main(root)

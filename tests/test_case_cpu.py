@@ -9,10 +9,12 @@ import os
 import pytest
 
 from fvens_gb300 import case
+from oracle import orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
-REF_TESTCASES = "/root/reference/testcases"
+_REF = orc.reference_root()
+REF_TESTCASES = os.path.join(_REF, "testcases") if _REF else ""
 
 
 def test_info_parser_nesting_comments_quotes():

@@ -13,7 +13,8 @@ from oracle import orc
 from tests import cases
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_MESHES = "/root/reference/tests/common-input"
+_REF = orc.reference_root()
+REF_MESHES = os.path.join(_REF, "tests", "common-input") if _REF else ""
 
 
 def test_library_exports_every_declared_symbol():
@@ -23,6 +24,12 @@ def test_library_exports_every_declared_symbol():
     assert len(names) > 30
     missing = [n for n in sorted(names) if not hasattr(L, n)]
     assert not missing, missing
+
+
+def test_abi_version_matches_header():
+    hdr = open(os.path.join(ROOT, "include", "fvens_gb300.h")).read()
+    v = int(re.search(r"#define FVENS_GB300_ABI_VERSION (\d+)", hdr).group(1))
+    assert fv.lib().fv_abi_version() == v == fv.ABI_VERSION
 
 
 def test_status_strings():
@@ -126,7 +133,7 @@ def test_faces_belong_to_their_cells(name):
         assert fn[f, 0] * (g["cc"][R, 0] - g["cc"][L, 0]) + fn[f, 1] * (g["cc"][R, 1] - g["cc"][L, 1]) > 0
 
 
-REF_TESTCASES = os.path.join(os.path.dirname(REF_MESHES), "..", "testcases") if REF_MESHES else ""
+REF_TESTCASES = os.path.join(_REF, "testcases") if _REF else ""
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_TESTCASES), reason="reference test cases not present")

@@ -36,10 +36,24 @@ def test_static_scratch_residual_matches_two_calls(cuda, mesh, phys, num, bcs):
         gd.compute_residual(u, r_ref, True, dt_ref)
         r = torch.zeros_like(u)
         dt = torch.zeros_like(dt_ref)
+        torch.cuda.synchronize()
+        if call == 0:
+            # the process's first call loads the array with the library's
+            # device image (a one-time, load-time reservation); every call
+            # from then on must leave the device's free memory as it was
+            assert _static_residual(gd, u, r, dt) == fv.FV_OK
+            torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(cuda)[0]
         assert _static_residual(gd, u, r, dt) == fv.FV_OK
         torch.cuda.synchronize()
+        # the device's free memory (driver view) is unchanged by the call
+        assert torch.cuda.mem_get_info(cuda)[0] == free0, f"call {call}: device memory was allocated"
         assert torch.equal(r, r_ref), f"call {call}: residuals differ"
         assert torch.equal(dt, dt_ref), f"call {call}: time steps differ"
+        # the handle's own scratch is untouched: its next evaluation is unchanged
+        r2 = torch.zeros_like(u)
+        gd.compute_residual(u, r2, True, dt_ref)
+        assert torch.equal(r2, r_ref), f"call {call}: the handle's own evaluation changed"
 
 
 def test_static_scratch_rejects_oversized(cuda):
