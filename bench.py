@@ -16,13 +16,24 @@ preconditioner.  Synthetic mesh and inputs (seeded generator); the working set
 explicit flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --kernel residual|ilu|jacobian|mpnn|fp64peak [--reps R]
+
+--impl reference: the oracle (the CPU FP64 restatement of the reference's
+path, natural-order ILU(0) as PETSc's) on all host cores, building the same
+mesh with its own generator; it times ONE complete solve of the workload (it
+takes minutes), whatever --steps / --warmup ask for, and says so in its line.
+
+--kernel: profiling aid; runs R launches of one kernel family on the workload
+(or on the laminar hybrid mesh for mpnn) and prints the mean time per launch.
 
 Prints one JSON line on rank 0 (N > 1: one independent solve per rank,
 weak scaling, no collective on the data path).
 """
 import argparse
+import hashlib
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -35,6 +46,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 MESH = [512, 256, 30.0, 0, 0, 1.02, 154, 3]
+SMALL_MESH = [64, 32, 30.0, 0, 0, 1.1, 20, 3]
 PHYS = dict(Minf=0.8, aoa_deg=1.25)
 NUM_MAIN = dict(flux="HLLC", gradient="GREENGAUSS", reconstruction="VENKATAKRISHNAN", limiter_param=5.0)
 NUM_START = dict(flux="HLLC", gradient="NONE")
@@ -44,10 +56,29 @@ STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_tim
 MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
             min_relax=0.2, pc="ilu0", matrix_free=1)
 WORKLOAD = "naca0012_transonic_512x256_ogrid_g1.02_hllc_gg_venkat5"
-# DRAM bytes (read + write) per launch from one ncu capture of this workload
-# (profiles/naca0012_c2_main_solve_launch_list.md; the gradient pass counts k_grad only)
-NCU_DRAM_BYTES = {"face_flux": 44611840, "gradients": 37975808}
 METRIC = "solves/s to ||R||<1e-10 (transonic NACA0012, matrix-free FGMRES, FP32 Jacobian + FP32 block-colour ILU0)"
+C2_FIXTURE = os.path.join(ROOT, "tests", "golden", "naca0012_transonic_oracle_converged.npz")
+
+# Per-launch counters of the residual's two heavy kernels on this workload
+# (ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,
+#  sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum,
+#  sm__thread_inst_executed_pipe_fp64_pred_on.sum on `python bench.py --kernel residual`),
+# valid for the kernel sources whose digest is `sources`; any other build reports them as null.
+NCU_COUNTS = {
+    "sources": None,
+    "face_flux": None,
+    "gradients": None,
+}
+KERNEL_SOURCES = ["fvens_gb300/csrc/fv_residual_body.cuh", "fvens_gb300/csrc/fv_device.cuh",
+                  "fvens_gb300/csrc/fv_residual.cu", "fvens_gb300/csrc/fv_core.cuh"]
+
+
+def kernel_sources_digest():
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def _dist():
@@ -55,6 +86,20 @@ def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def workload_config(world, small=False):
+    """The workload's description, identical in both arms' lines."""
+    mesh = SMALL_MESH if small else MESH
+    return {"workload": WORKLOAD if not small else "naca0012_transonic_64x32_ogrid_g1.1_hllc_gg_venkat5_test",
+            "mesh": f"NACA 0012 O-grid {mesh[0]} x {mesh[1]} to {mesh[2]:g} chords, radial growth {mesh[5]:g}, "
+                    f"rings from {mesh[6]} triangulated (seed {mesh[7]})",
+            "cells": 183296 if not small else 2 * 64 * 32 - 20 * 64, "faces": 314880 if not small else None,
+            "flow": "inviscid, M 0.8, AoA 1.25 deg", "scheme": "HLLC, Green-Gauss, Venkatakrishnan K=5",
+            "solve": "freestream; 100 first-order starter steps (CFL 25->500); second-order solve to "
+                     "||R||<1e-10 (CFL 100->5000, matrix-free FGMRES(30))",
+            "batch": 1, "parallelism": f"replicas{world}" if world > 1 else "single",
+            "l2": "working set > L2 (no flush needed)"}
 
 
 class ClockSampler:
@@ -102,8 +147,15 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def build_case(fv):
-    m = fv.UMesh.generate(fv.MESH_NACA_OGRID, MESH, reorder=1)
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def build_case(fv, small=False):
+    m = fv.UMesh.generate(fv.MESH_NACA_OGRID, SMALL_MESH if small else MESH, reorder=1)
     ph = fv.physics_cfg(**PHYS)
     main = fv.FlowFV(m, ph, fv.numerics_cfg(**NUM_MAIN), BCS)
     start = fv.FlowFV(m, ph, fv.numerics_cfg(**NUM_START), BCS)
@@ -123,7 +175,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     reps = Replicas("nccl", dev)
-    m, main, start = build_case(fv)
+    m, main, start = build_case(fv, args.small)
     prec = 8 if args.plain else 4
     S1 = fv.SteadyBackwardEulerSolver(start, precision=prec, **STARTER)
     S2 = fv.SteadyBackwardEulerSolver(main, precision=prec, **MAIN)
@@ -166,27 +218,28 @@ def run_ours(args):
     value = reps.throughput(args.steps, ms / 1e3)
     ms = reps.max_over_ranks(ms)
     converged = all(s2["status"] == 0 for _, s2 in stats)
+    u_conv = ud.clone()
 
     # end to end through the host-buffer C-ABI call: pinned host state in,
     # converged state out (starter and main solve)
+    n_e2e = max(1, min(args.steps, args.e2e_solves))
     hu = torch.empty((m.nelem, 4), dtype=torch.float64).pin_memory()
     hn = hu.numpy()
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(n_e2e):
         hn[:] = u0
         S1.solve_host(hn, raise_on_error=False)
         S2.solve_host(hn, raise_on_error=False)
     t1 = time.perf_counter()
-    e2e_value = reps.throughput(args.steps, t1 - t0)
-    cl = main.surface_data(ud, 2)[0]
-    u_conv = ud.clone()
+    e2e_value = reps.throughput(n_e2e, t1 - t0)
+    cl = main.surface_data(u_conv, 2)[0]
     variants = {} if args.no_variants else run_variants(fv, torch, dev, m, main, start, u0d, prec, args)
     ud.copy_(u_conv)
 
-    # per-kernel timing (roofline) at the converged state; time shares of one
-    # solve from the launch counts per step / per Krylov iteration
+    # per-kernel timing at the converged state; time shares of one solve from
+    # the launch counts per step / per Krylov iteration
     def timed(S, which, reps=20):
         import ctypes
         a, b = ctypes.c_double(), ctypes.c_double()
@@ -211,13 +264,10 @@ def run_ours(args):
               "gradients": calls["residual"] * kern["gradients"]["ms"],
               "ilu0_apply": share_ms["ilu0_apply"]}
     dom = max(single, key=single.get)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    peaks = _peaks()
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    dfma_rate, _ = fv.fp64_peak(5)
     nf = m.naface
     nblocks = m.nelem + 2 * (m.naface - m.nbface)
     line = {
@@ -233,36 +283,60 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f64 residual+krylov / f32 jacobian+ilu0" if prec == 4 else "f64",
         "data": "synthetic (seeded NACA 0012 O-grid generator, freestream start)",
-        "config": {"workload": WORKLOAD, "cells": m.nelem, "faces": nf, "batch": 1,
-                   "parallelism": f"replicas{world}" if world > 1 else "single",
-                   "l2": "working set > L2 (no flush needed)",
-                   "starter_steps": s1["steps"], "main_steps": steps_main, "linear_iters": lin_main,
-                   "converged": converged, "final_res": s2["res"],
-                   "cl_cdp": [float(cl[0]), float(cl[1])],
-                   "residual_block_sizes": block_sizes},
+        "config": workload_config(world, args.small),
+        "solve": {"starter_steps": s1["steps"], "starter_linear_iters": s1["lin_iters"], "main_steps": steps_main,
+                  "linear_iters": lin_main, "converged": converged, "final_res": s2["res"],
+                  "cl_cdp": [float(cl[0]), float(cl[1])], "residual_block_sizes": block_sizes,
+                  "launches_per_solve": launches / max(args.steps, 1)},
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(u0.nbytes),
-                "d2h_bytes_per_step": int(u0.nbytes)},
+                "d2h_bytes_per_step": int(u0.nbytes), "solves": n_e2e},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": hbm_peak,
-                     "unit": "GB/s", "frac": kern[dom]["gbs"] / hbm_peak,
-                     "traffic": NCU_DRAM_BYTES.get(dom), "peak_source": peak_src,
-                     "note": "FP64-pipe bound (ncu: FP64 pipe 87 % busy, DRAM 4 %)" if dom != "ilu0_apply" else
-                             "latency bound level walk"},
+        "roofline": roofline(dom, kern, nf, hbm_peak, peak_src, dfma_rate),
         "kernels": kern,
         "solve_time_shares_ms": share_ms,
         "variants": variants,
         "residual_gfaces_s": nf / (kern["residual"]["ms"] * 1e-3) / 1e9,
         "jacobian_blocks_s": nblocks / (kern["jacobian"]["ms"] * 1e-3),
         "ilu0_sweep_gbs": kern["ilu0_apply"]["gbs"],
+        "fp64_peak_tflops": 2 * dfma_rate / 1e12,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu:
         u_host = u_conv.cpu().numpy().reshape(m.nelem, 4)
-        line["cpu_baseline"] = cpu_baseline(m, s1, s2, args.cpu_seconds, u_host)
+        line["cpu_baseline"] = cpu_baseline(m, args.cpu_seconds, u_host)
         line["oracle_parity"] = oracle_parity(m, main, u_conv)
     if rank == 0:
         print(json.dumps(line), flush=True)
     reps.close()
+
+
+def roofline(dom, kern, nfaces, hbm_peak, peak_src, dfma_rate):
+    """The roofline of the dominant kernel.  The residual's kernels are bound
+    by the FP64 pipe on this part: FLOP/s (DADD + DMUL + 2 DFMA per launch,
+    from the ncu counters of this build) against twice the measured DFMA rate,
+    with the FP64-pipe instruction rate against the DFMA rate beside it; the
+    HBM fraction of the model bytes is reported too.  The ILU(0) sweep is
+    reported against HBM."""
+    k = kern[dom]
+    hbm = {"achieved": k["gbs"], "peak": hbm_peak, "unit": "GB/s", "frac": k["gbs"] / hbm_peak,
+           "peak_source": peak_src}
+    valid = NCU_COUNTS["sources"] == kernel_sources_digest()
+    cnt = NCU_COUNTS.get(dom) if valid else None
+    traffic = cnt["dram_bytes"] if cnt else None
+    if dom == "ilu0_apply" or cnt is None:
+        out = dict(bound="hbm", kernel=dom, traffic=traffic, **hbm)
+        if dom != "ilu0_apply":
+            out["note"] = "FP64-pipe bound; no ncu capture of this build's kernel sources to count its FP64 work"
+        return out
+    sec = k["ms"] * 1e-3
+    flops = cnt["fp64_flop"] * nfaces / cnt["faces"]
+    pipe = cnt["fp64_pipe_inst"] * nfaces / cnt["faces"]
+    peak = 2 * dfma_rate
+    return {"bound": "fp64", "kernel": dom, "achieved": flops / sec / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+            "frac": flops / sec / peak, "fp64_pipe_frac": pipe / sec / dfma_rate,
+            "traffic": traffic, "peak_source": "measured in this run (fv_fp64_peak: FP64 FMA chains on every SM)",
+            "counts_per_launch": {"fp64_flop": flops, "fp64_pipe_inst": pipe, "source": cnt["capture"]},
+            "hbm": hbm}
 
 
 def _timed_solve(torch, S_list, u, all_members=False):
@@ -280,7 +354,8 @@ def _timed_solve(torch, S_list, u, all_members=False):
 def run_variants(fv, torch, dev, m, main, start, u0d, prec, args):
     """(1) The same solve on the plain path: FP64 Jacobian and FP64 ILU(0),
     freestream start, one timed solve (CUDA events).  (2) Batched laminar
-    solves (run_batched)."""
+    solves (run_batched).  (3) The learned warm start (run_warm_start).
+    (4) The ~4M-cell instance (run_large)."""
     out = {}
     u = torch.empty_like(u0d)
     P1 = fv.SteadyBackwardEulerSolver(start, precision=8, **STARTER)
@@ -291,28 +366,30 @@ def run_variants(fv, torch, dev, m, main, start, u0d, prec, args):
                               "linear_iters": st["lin_iters"], "converged": st["status"] == 0, "res": st["res"]}
     del P1, P2
     if args.large:
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except Exception:
-            pass
-        out["large_4m_kernels"] = run_large(fv, torch, dev, float(peaks.get("hbm_gbs", 6800.0)))
-    out["batched_laminar"] = bl = run_batched(fv, torch, dev)
-    if args.warm_train > 0:
-        out["warm_start_laminar"] = run_warm_start(fv, torch, dev, args.warm_train, args.warm_test, args.warm_epochs,
-                                                   plain_single_s=bl["single_plain_fp64"]["seconds"])
+        out["large_4m"] = run_large(fv, torch, dev, float(_peaks().get("hbm_gbs", 6800.0)), args.large_solve)
+    if args.batched:
+        out["batched_laminar"] = bl = run_batched(fv, torch, dev, args.laminar_levels, args.batch)
+        if args.warm_train > 0:
+            out["warm_start_laminar"] = run_warm_start(
+                fv, torch, dev, args.laminar_levels, args.warm_train, args.warm_test, args.warm_epochs, args.batch,
+                plain_single_s=bl["single_plain_fp64"]["seconds"])
     return out
 
 
 LAMINAR_BCS = [(4, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))]
+LAMINAR_FIXTURE = os.path.join(ROOT, "tests", "golden", "naca0012_laminar_l{}_oracle_converged.npz")
 
 
-def _laminar_mesh(fv):
-    """The reference's hybrid NACA 0012 mesh (13,156 cells) with its
-    boundary-layer lines kept whole in the preconditioner's parts."""
+def _laminar_mesh(fv, levels=0):
+    """The reference's hybrid NACA 0012 mesh (13,156 cells), uniformly refined
+    `levels` times by the rule that makes the reference's level-2 mesh from
+    it (13,156 x 4^levels cells), with its boundary-layer lines kept whole in
+    the preconditioner's parts."""
+    from fvens_gb300 import meshes
     z = np.load(os.path.join(ROOT, "tests", "golden", "naca0012_lam_hybrid_1_mesh.npz"))
-    m = fv.UMesh.from_arrays(z["coords"], z["nnode"].astype(np.int32), z["inpoel"], z["bface"],
-                             z["btag"].astype(np.int32), reorder=1)
+    a = meshes.refine(dict(coords=z["coords"], nnode=z["nnode"], inpoel=z["inpoel"], bface=z["bface"],
+                           btag=z["btag"]), levels)
+    m = fv.UMesh.from_arrays(a["coords"], a["nnode"], a["inpoel"], a["bface"], a["btag"], reorder=1)
     return m, m.find_lines(10.0)[0]
 
 
@@ -325,18 +402,20 @@ def _laminar_conditions(fv, n, seed):
                            viscous=True) for k in range(n)]
 
 
+LAMINAR_MAIN = dict(cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=1500, nl_update=2)
+LAMINAR_START = dict(cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0, max_timesteps=50, nl_update=2)
+
+
 def _laminar_solvers(fv, m, plist, prec, starter=True, pc="ilu0"):
     """(discretisation, [starter solver,] main solver) for the conditions plist:
     first-order starter to a relative 1e-1 (at most 50 steps), then the
     second-order main solve to the absolute 1e-10."""
     main = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), LAMINAR_BCS)
-    S2 = fv.SteadyBackwardEulerSolver(main, cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
-                                      max_timesteps=600, pc=pc, nl_update=2, precision=prec)
+    S2 = fv.SteadyBackwardEulerSolver(main, pc=pc, precision=prec, **LAMINAR_MAIN)
     if not starter:
         return main, [S2]
     start = fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS)
-    S1 = fv.SteadyBackwardEulerSolver(start, cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0,
-                                      max_timesteps=50, pc=pc, nl_update=2, precision=prec)
+    S1 = fv.SteadyBackwardEulerSolver(start, pc=pc, precision=prec, **LAMINAR_START)
     return main, [S1, S2]
 
 
@@ -344,31 +423,62 @@ def _freestream_field(torch, dev, disc, nelem):
     return torch.tensor(np.concatenate([np.tile(x, (nelem, 1)) for x in disc.freestream()]), device=dev)
 
 
-def run_batched(fv, torch, dev, B=64, seed=7):
+def _vs_laminar_fixture(m, levels, main, u, members):
+    """Converged states and Cl / CDp / CDsf of the given batch members against
+    the oracle's own converged solves of the same conditions (committed
+    fixture; None when absent)."""
+    path = LAMINAR_FIXTURE.format(levels)
+    if not os.path.exists(path):
+        return None
+    z = np.load(path)
+    perm = m.export()["perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(len(perm))
+    uv = u.view(-1, m.nelem, 4).cpu().numpy()
+    fun = main.surface_data(u, 2)
+    out = []
+    for j, k in enumerate(z["members"]):
+        if k not in members:
+            continue
+        ug = uv[k][inv[z["cells"]]]
+        uo = z["states"][j]
+        out.append({"member": int(k), "state_rel_diff": float(np.abs(ug - uo).max() / np.abs(uo).max()),
+                    "cl_cdp_cdsf_rel_diff": [float(abs(fun[k, i] - z["functionals"][j, i]) /
+                                                   max(abs(z["functionals"][j, i]), 1e-300)) for i in range(3)]})
+    return out
+
+
+def run_batched(fv, torch, dev, levels=2, B=64, seed=7):
     """Batched solves of B laminar conditions (M ~ U[0.3, 0.7], AoA ~ U[-4, 4] deg,
     Re ~ U[2000, 10000], Pr 0.72, adiabatic wall; Roe, least squares) on the
-    reference's hybrid NACA 0012 mesh (13,156 cells), all members in the same
-    launches with FP32 Jacobians and ILU(0) (and with block SGS), against one
-    member alone on the FP32 path and on the plain FP64 path."""
+    reference's hybrid NACA 0012 mesh refined `levels` times, all members in
+    the same launches with FP32 Jacobians and block SGS (and with ILU(0)),
+    against member 0 alone on the FP32 path and on the plain FP64 path."""
     import collections
-    m, nlines = _laminar_mesh(fv)
+    m, nlines = _laminar_mesh(fv, levels)
     phs = _laminar_conditions(fv, B, seed)
-    res = {"mesh_cells": m.nelem, "batch": B, "lines": nlines}
+    res = {"mesh_cells": m.nelem, "mesh_faces": m.naface, "refinements": levels, "batch": B, "lines": nlines}
     for tag, plist, prec, pc in (("single_plain_fp64", phs[:1], 8, "ilu0"), ("single", phs[:1], 4, "ilu0"),
-                                 ("batch", phs, 4, "ilu0"), ("batch_sgs", phs, 4, "sgs")):
+                                 ("batch_sgs", phs, 4, "sgs"), ("batch", phs, 4, "ilu0")):
         main, solvers = _laminar_solvers(fv, m, plist, prec, pc=pc)
         u = _freestream_field(torch, dev, main, m.nelem)
         t, stats = _timed_solve(torch, solvers, u, all_members=True)
         conv = sum(1 for st in stats if st["status"] == 0)
         res[tag] = {"seconds": t, "converged": conv, "members": len(plist), "converged_solves_s": conv / t,
                     "status_counts": dict(collections.Counter(int(st["status"]) for st in stats)),
-                    "main_steps_max": max(st["steps"] for st in stats)}
-    res["batch_vs_single_plain_fp64"] = (res["batch"]["converged_solves_s"] /
-                                         max(res["single_plain_fp64"]["converged_solves_s"], 1e-30))
+                    "main_steps_max": max(st["steps"] for st in stats),
+                    "main_steps_mean": float(np.mean([st["steps"] for st in stats])),
+                    "linear_iters_mean": float(np.mean([st["lin_iters"] for st in stats]))}
+        if tag in ("single_plain_fp64", "batch"):
+            res[tag]["vs_oracle"] = _vs_laminar_fixture(m, levels, main, u,
+                                                        [k for k, st in enumerate(stats) if st["status"] == 0])
+        del main, solvers, u
+    best = max(res["batch"]["converged_solves_s"], res["batch_sgs"]["converged_solves_s"])
+    res["batch_vs_single_plain_fp64"] = best / max(res["single_plain_fp64"]["converged_solves_s"], 1e-30)
     return res
 
 
-def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s=None):
+def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_single_s=None):
     """Learned warm start on the laminar hybrid NACA 0012 case.
 
     n_train conditions (seed 11) are solved in batches of B from freestream
@@ -376,18 +486,18 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
     (4 layers, width 64; BF16 tensor-core GEMMs, FP32 accumulation, Adam) on
     the GPU.  n_test held-out conditions (seed 12, same distributions) are then
     solved twice in batches of B on the FP32-preconditioned path: from
-    freestream with the starter, and from the network's prediction without it.
-    Reported: nonlinear steps, wall time (CUDA events), initial-state error
-    relative to the converged state, the largest difference of the two
-    converged states and of their Cl/Cd, and the warm-started batch's rate
-    against one plain FP64 solve."""
+    freestream with the starter, and from the network's prediction without it
+    (members that do not converge fall back to freestream).  Reported:
+    nonlinear steps, wall time (CUDA events), initial-state error relative to
+    the converged state, the largest difference of the two converged states
+    and of their Cl/Cd, and the warm-started batch's rate against one plain
+    FP64 solve."""
     import collections
 
     from fvens_gb300.mpnn import MPNN, fallback_solve, output_scale, train
-    m, _ = _laminar_mesh(fv)
+    m, _ = _laminar_mesh(fv, levels)
     phs_tr = _laminar_conditions(fv, n_train, 11)
     phs_te = _laminar_conditions(fv, n_test, 12)
-    # training data: converged states of the batched solver
     ev = lambda: torch.cuda.Event(enable_timing=True)
     keep_phys, keep_u, gen_s = [], [], 0.0
     for s in range(0, n_train, B):
@@ -401,7 +511,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
             if st["status"] == 0:
                 keep_phys.append(plist[k])
                 keep_u.append(uv[k].clone())
-        del main, solvers
+        del main, solvers, u
     targets = torch.stack(keep_u)
     uinf = np.array([[1.0, np.cos(p.aoa), np.sin(p.aoa), 1.0 / (p.gamma * p.Minf ** 2) / (p.gamma - 1) + 0.5]
                      for p in keep_phys])
@@ -413,10 +523,10 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
     b.record()
     torch.cuda.synchronize()
     train_s = a.elapsed_time(b) / 1e3
-    # held-out conditions: freestream + starter vs prediction, batches of B
-    out = {"train_conditions": n_train, "train_converged": len(keep_phys), "test_conditions": n_test,
-           "epochs": epochs, "train_batch": 16, "params": net.nparams, "data_generation_s": gen_s,
-           "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
+    del targets, keep_u
+    out = {"mesh_cells": m.nelem, "train_conditions": n_train, "train_converged": len(keep_phys),
+           "test_conditions": n_test, "epochs": epochs, "train_batch": 16, "params": net.nparams,
+           "data_generation_s": gen_s, "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
     agg = {k: dict(seconds=0.0, steps=[], res0=[], status=collections.Counter()) for k in ("freestream", "warm")}
     fb = dict(seconds=0.0, members=0, converged=0)
     err_ratio, du, dcl, dcd, pred_s = [], [], [], [], 0.0
@@ -442,8 +552,8 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
         # the network's result judged: members that did not converge restart from freestream
         st_fb = [dict(x) for x in st_warm]
         starter_fb = fv.SteadyBackwardEulerSolver(
-            fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS), cfl_min=200,
-            cfl_max=1000, tolerance=1e-1, abs_tolerance=0, max_timesteps=50, pc="ilu0", nl_update=2, precision=4)
+            fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS), pc="ilu0", precision=4,
+            **LAMINAR_START)
         u_fb = u_warm.clone()
         a2, b2 = ev(), ev()
         a2.record()
@@ -453,8 +563,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
         fb["seconds"] += a2.elapsed_time(b2) / 1e3
         fb["members"] += len(fell)
         fb["converged"] += sum(1 for x in st_fb if x["status"] == 0)
-        del starter_fb
-        # freestream stats from the main solver (the starter's steps added)
+        del starter_fb, u_fb
         for tag, sts in (("freestream", st_free), ("warm", st_warm)):
             agg[tag]["status"].update(int(x["status"]) for x in sts)
             agg[tag]["steps"] += [int(x["steps"]) for x in sts]
@@ -476,7 +585,7 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
             if st_free[k]["status"] == 0 and st_warm[k]["status"] == 0:
                 dcl.append(float(abs(cw[k, 0] - cf[k, 0])))
                 dcd.append(float(abs(cw[k, 1] - cf[k, 1]) / abs(cf[k, 1])))
-        del main, solvers, main_w, solvers_w
+        del main, solvers, main_w, solvers_w, u_free, u0_free, u_warm, u0_warm
     for tag in agg:
         conv = agg[tag]["status"].get(0, 0)
         st = agg[tag]
@@ -486,13 +595,11 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
                     "status_counts": {str(k): v for k, v in st["status"].items()}}
     out["freestream"]["note"] = "main-solve steps; a first-order starter ran before each batch"
     out["warm"]["prediction_s"] = pred_s
-    # with the fallback: the members the warm start did not converge, solved again from freestream
     fb_s = out["warm"]["seconds"] + fb["seconds"]
     out["warm_with_fallback"] = {"seconds": fb_s, "converged": fb["converged"], "fallback_members": fb["members"],
                                  "fallback_s": fb["seconds"], "converged_solves_s": fb["converged"] / fb_s}
     out["initial_error_ratio_mean"] = float(np.mean(err_ratio)) if err_ratio else None
     out["initial_error_ratio_max"] = float(np.max(err_ratio)) if err_ratio else None
-    # both starts converged: how far apart are the two converged states?
     q = lambda v, f: float(np.quantile(v, f)) if v else None
     out["converged_state_rel_diff"] = {"median": q(du, 0.5), "p90": q(du, 0.9), "max": q(du, 1.0),
                                        "within_1e-8": sum(1 for x in du if x <= 1e-8), "members": len(du)}
@@ -500,6 +607,8 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
     out["cdp_rel_diff"] = {"median": q(dcd, 0.5), "max": q(dcd, 1.0),
                            "within_1e-8": sum(1 for x in dcd if x <= 1e-8)}
     out["warm_vs_freestream"] = out["warm"]["converged_solves_s"] / max(out["freestream"]["converged_solves_s"], 1e-30)
+    out["warm_with_fallback_vs_freestream"] = (out["warm_with_fallback"]["converged_solves_s"] /
+                                               max(out["freestream"]["converged_solves_s"], 1e-30))
     if plain_single_s:
         out["warm_batch_vs_single_plain_fp64"] = out["warm"]["converged_solves_s"] * plain_single_s
     return out
@@ -508,22 +617,30 @@ def run_warm_start(fv, torch, dev, n_train, n_test, epochs, B=64, plain_single_s
 LARGE_MESH = [2048, 1024, 20.0, 96, 2e-5, 1.05, 96, 9]
 
 
-def run_large(fv, torch, dev, peak_gbs):
-    """Large single-instance kernel throughput: hybrid NACA 0012 viscous mesh of
-    2048 x 1024 O-grid cells (96 quad boundary-layer rings from 2e-5 chords,
-    growth 1.05; triangles outside; 3,997,696 cells), M 0.75, AoA 2 deg,
-    Re 5000; HLLC, least squares, Barth-Jespersen.  Each kernel is timed alone
-    (CUDA events, an L2 eviction before every launch) at a perturbed freestream
-    state: residual Gfaces/s, Jacobian blocks/s, FP32 ILU(0) apply GB/s, as
-    fractions of the HBM copy peak."""
-    import ctypes
-    t0 = time.perf_counter()
+def _large_case(fv):
     m = fv.UMesh.generate(fv.MESH_NACA_OGRID, LARGE_MESH, reorder=1)
-    t_mesh = time.perf_counter() - t0
     ph = fv.physics_cfg(Minf=0.75, aoa_deg=2.0, Reinf=5000.0, Tinf=288.15, Pr=0.72, viscous=True)
     bcs = [(2, "adiabaticwall", (0.0,)), (4, "farfield", ())]
     main = fv.FlowFV(m, ph, fv.numerics_cfg(flux="HLLC", gradient="LEASTSQUARES", reconstruction="BARTHJESPERSEN"),
                      bcs)
+    start = fv.FlowFV(m, ph, fv.numerics_cfg(flux="HLLC", gradient="NONE"), bcs)
+    return m, main, start
+
+
+def run_large(fv, torch, dev, peak_gbs, solve=True):
+    """Large single instance: hybrid NACA 0012 viscous mesh of 2048 x 1024
+    O-grid cells (96 quad boundary-layer rings from 2e-5 chords, growth 1.05;
+    triangles outside; 3,997,696 cells), M 0.75, AoA 2 deg, Re 5000; HLLC,
+    least squares, Barth-Jespersen.  Each kernel is timed alone (CUDA events,
+    an L2 eviction before every launch) at a perturbed freestream state:
+    residual Gfaces/s, Jacobian blocks/s, FP32 ILU(0) apply GB/s, as fractions
+    of the HBM copy peak.  With solve: the end-to-end solve from freestream
+    (starter + main to ||R|| < 1e-10) on the FP32-preconditioned path and on
+    the plain FP64 path."""
+    import ctypes
+    t0 = time.perf_counter()
+    m, main, start = _large_case(fv)
+    t_mesh = time.perf_counter() - t0
     S = fv.SteadyBackwardEulerSolver(main, cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1,
                                      max_timesteps=1, pc="ilu0", precision=4, matrix_free=1)
     rng = np.random.default_rng(3)
@@ -542,15 +659,60 @@ def run_large(fv, torch, dev, peak_gbs):
     out["residual_gfaces_s"] = m.naface / (out["residual"]["ms"] * 1e-3) / 1e9
     out["jacobian_blocks_s"] = nb / (out["jacobian"]["ms"] * 1e-3)
     out["ilu0_sweep_gbs"] = out["ilu0_apply"]["gbs"]
+    del S
+    if solve:
+        for tag, prec in (("solve_fp32_precond", 4), ("solve_plain_fp64", 8)):
+            S1 = fv.SteadyBackwardEulerSolver(start, precision=prec, **LARGE_STARTER)
+            S2 = fv.SteadyBackwardEulerSolver(main, precision=prec, **LARGE_MAIN)
+            u.copy_(torch.tensor(np.tile(main.freestream()[0], (m.nelem, 1)), device=dev))
+            t, st = _timed_solve(torch, [S1, S2], u)
+            cl = main.surface_data(u, 2)[0]
+            out[tag] = {"solve_s": t, "main_steps": st["steps"], "linear_iters": st["lin_iters"],
+                        "status": st["status"], "res": st["res"], "cl_cdp_cdsf": [float(x) for x in cl]}
+            del S1, S2
+        a, b = out["solve_fp32_precond"], out["solve_plain_fp64"]
+        if a["status"] == 0 and b["status"] == 0:
+            out["fp32_vs_plain_fp64"] = b["solve_s"] / a["solve_s"]
     return out
 
 
-def _oracle_case(m):
+LARGE_STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
+                     min_relax=0.2, pc="ilu0")
+LARGE_MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=1500, nl_update=2,
+                  min_relax=0.2, pc="ilu0", matrix_free=1)
+
+
+# ----------------------------- oracle legs ----------------------------------
+
+def _oracle_case_from_arrays(arrs):
     from oracle import orc
-    om = orc.Mesh.from_export(m.export())
+    om = orc.Mesh(arrs["coords"], arrs["nnode"], arrs["inpoel"], arrs["bface"], arrs["btag"])
     od1 = orc.Disc(om, **PHYS, **NUM_START, bcs=BCS)
     od2 = orc.Disc(om, **PHYS, **NUM_MAIN, bcs=BCS)
+    return om, od1, od2
+
+
+def _oracle_case(m):
+    """Oracle discretisations on the product mesh m (same cell order)."""
+    _, od1, od2 = _oracle_case_from_arrays(m.export())
     return od1, od2
+
+
+def oracle_solve(od1, od2, u):
+    """One complete solve of the workload on the oracle: the starter and the
+    main solve with the workload's settings, natural-order ILU(0) as PETSc's.
+    Returns (u, starter stats, main stats, starter seconds, main seconds)."""
+    S, M = STARTER, MAIN
+    t0 = time.perf_counter()
+    u, st1 = od1.steady_solve(u, cflmin=S["cfl_min"], cflmax=S["cfl_max"], tol=S["tolerance"],
+                              maxiter=S["max_timesteps"], abs_tol=bool(S["abs_tolerance"]), pc="ilu0",
+                              nl_update="bounded", min_relax=S["min_relax"])
+    t1 = time.perf_counter()
+    u, st2 = od2.steady_solve(u, cflmin=M["cfl_min"], cflmax=M["cfl_max"], tol=M["tolerance"],
+                              maxiter=M["max_timesteps"], abs_tol=bool(M["abs_tolerance"]), pc="ilu0",
+                              nl_update="bounded", min_relax=M["min_relax"], matrix_free=bool(M["matrix_free"]))
+    t2 = time.perf_counter()
+    return u, st1, st2, t1 - t0, t2 - t1
 
 
 def _oracle_steps(od, cfg, u, nsteps, lin_maxit):
@@ -574,13 +736,26 @@ def _oracle_step_model(od, cfg, u, budget_s):
     return t1 - b, b, n
 
 
+def _fixture_counts():
+    """Step and Krylov counts of the oracle's own complete solve of the
+    workload (recorded with the committed converged-state fixture)."""
+    if not os.path.exists(C2_FIXTURE):
+        return None
+    z = np.load(C2_FIXTURE)
+    s = z["solve_counts"]
+    return {"starter": {"steps": int(s[0]), "lin_iters": int(s[1])}, "main": {"steps": int(s[2]),
+                                                                              "lin_iters": int(s[3])},
+            "recorded_seconds": float(z["solve_seconds"]), "recorded_threads": int(z["solve_threads"])}
+
+
 def oracle_parity(m, main, ud):
-    """The GPU's numbers on this workload against the oracle on the same mesh and
-    state: the second-order residual at the converged state and at a seeded
-    5 % perturbation of freestream (max |difference| over the largest sum of
-    |face flux x length| of a cell), and Cl, CDp at the converged state."""
+    """The GPU's numbers on this workload against the oracle: the
+    second-order residual at the GPU's converged state and at a seeded 5 %
+    perturbation of freestream (max |difference| over the largest sum of
+    |face flux x length| of a cell), Cl, CDp at the converged state, and the
+    converged state and Cl, CDp against the oracle's own complete solve of
+    the workload (committed fixture: the state at sampled cells)."""
     import torch
-    from oracle import orc
     _, od2 = _oracle_case(m)
     out = {}
     u_conv = ud.detach().cpu().numpy().reshape(m.nelem, 4)
@@ -596,26 +771,42 @@ def oracle_parity(m, main, ud):
     cg = main.surface_data(ud, 2)[0]
     co = od2.surface_data(u_conv, 2)
     out["cl_cdp_rel_err"] = [float(abs(cg[k] - co[k]) / abs(co[k])) for k in (0, 1)]
+    if os.path.exists(C2_FIXTURE) and m.nelem == 183296:
+        z = np.load(C2_FIXTURE)
+        perm = m.export()["perm"]
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(len(perm))
+        ug = u_conv[inv[z["cells"]]]
+        uo = z["states"]
+        out["vs_oracle_converged_solve"] = {
+            "state_rel_diff": float(np.abs(ug - uo).max() / np.abs(uo).max()),
+            "cells_compared": int(len(z["cells"])),
+            "cl_cdp_rel_diff": [float(abs(cg[k] - z["functionals"][k]) / abs(z["functionals"][k])) for k in (0, 1)]}
     return out
 
 
-def cpu_baseline(m, starter, main, budget_s, u_state=None):
+def cpu_baseline(m, budget_s, u_state=None, counts=None):
     """The oracle (the CPU restatement of the reference's path, natural-order
-    ILU(0) as PETSc's) on the host cores: a bounded sample of pseudo-time
+    ILU(0) as PETSc's) on the host cores, on a bounded sample: pseudo-time
     steps of the starter and of the main solve with pinned FGMRES iteration
-    counts gives the cost per step and per Krylov iteration, which is applied
-    to the step and iteration counts of the GPU solve.  starter / main: the
-    GPU's fv_solve_stats of the two solves.  With u_state (host array of the
-    state the GPU kernels were timed at), the oracle's residual, FP64 Jacobian
-    assembly, ILU(0) factorisation and ILU(0) apply are timed there too."""
+    counts give the cost per step and per Krylov iteration, scaled to the step
+    and Krylov counts of the oracle's own complete solve of the workload
+    (counts: {"starter": {...}, "main": {...}}; default: the committed
+    fixture's record).  With u_state (host array of the state the GPU kernels
+    were timed at), the oracle's residual, FP64 Jacobian assembly, ILU(0)
+    factorisation and ILU(0) apply are timed there too."""
     from oracle import orc
     nthreads = os.cpu_count() or 1
     orc.set_threads(nthreads)
+    counts = counts or _fixture_counts()
+    if counts is None:
+        return {"unavailable": "no record of the oracle's complete solve (tests/golden fixture absent)"}
     od1, od2 = _oracle_case(m)
     u0 = np.tile(od2.freestream(), (m.nelem, 1))
     a1, b1, n1 = _oracle_step_model(od1, STARTER, u0, 0.4 * budget_s)
     a2, b2, n2 = _oracle_step_model(od2, MAIN, u0, 0.6 * budget_s)
-    solve_s = (a1 * starter["steps"] + b1 * starter["lin_iters"]) + (a2 * main["steps"] + b2 * main["lin_iters"])
+    st, mn = counts["starter"], counts["main"]
+    solve_s = (a1 * st["steps"] + b1 * st["lin_iters"]) + (a2 * mn["steps"] + b2 * mn["lin_iters"])
     kernels = {}
     if u_state is not None:
         t = od2.time_kernels(u_state, "ilu0", reps=5)
@@ -627,41 +818,143 @@ def cpu_baseline(m, starter, main, budget_s, u_state=None):
     return {"value": 1.0 / solve_s, "unit": "solves/s", "cores": nthreads, "kind": "port",
             "sample": f"2 x {n1} starter + 2 x {n2} main pseudo-time steps of the same workload on the oracle with "
                       f"1 and 8 FGMRES(30) iterations per step (natural-order ILU(0)); per step {a1:.3f} / {a2:.3f} s "
-                      f"+ per Krylov iteration {b1:.3f} / {b2:.3f} s, applied to {starter['steps']} + {main['steps']} "
-                      f"steps and {starter['lin_iters']} + {main['lin_iters']} Krylov iterations per solve", **kernels}
+                      f"+ per Krylov iteration {b1:.3f} / {b2:.3f} s, scaled to the oracle's own complete solve: "
+                      f"{st['steps']} + {mn['steps']} steps and {st['lin_iters']} + {mn['lin_iters']} Krylov "
+                      f"iterations (the reference arm times that solve whole)", **kernels}
 
 
 def run_reference(args):
     """The reference's CPU path as restated by the oracle (the reference itself
     does not build here: PETSc, Eigen, Boost and MPI are absent), on all host
-    threads; each step is a bounded sample of the workload."""
+    threads: ONE complete solve of the workload from freestream, timed whole
+    (mesh built by the oracle's own generator; the product library is not
+    loaded).  Under torchrun only rank 0 runs."""
     rank, world, local = _dist()
     if rank != 0:
         return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from fvens_gb300 import build as fvbuild
-    import fvens_gb300 as fv
     if not os.path.exists(fvbuild.ORACLE_LIB):
         fvbuild.build_oracle()
+    from oracle import meshgen, orc
+    nthreads = os.cpu_count() or 1
+    orc.set_threads(nthreads)
+    t0 = time.perf_counter()
+    arrs = meshgen.naca_ogrid(*(SMALL_MESH if args.small else MESH))
+    om, od1, od2 = _oracle_case_from_arrays(arrs)
+    t_mesh = time.perf_counter() - t0
+    u = np.tile(od2.freestream(), (om.nelem, 1))
+    u, st1, st2, ts, tm = oracle_solve(od1, od2, u)
+    solve_s = ts + tm
+    value = 1.0 / solve_s
+    fun = od2.surface_data(u, 2)
+    solve = {"starter_steps": st1["steps"], "starter_linear_iters": st1["lin_iters"], "main_steps": st2["steps"],
+             "linear_iters": st2["lin_iters"], "converged": st2["status"] == 0, "final_res": float(st2["res"]),
+             "cl_cdp": [float(fun[0]), float(fun[1])], "starter_s": ts, "main_s": tm, "mesh_setup_s": t_mesh}
+    if os.path.exists(C2_FIXTURE) and not args.small:
+        z = np.load(C2_FIXTURE)
+        solve["vs_committed_oracle_solve"] = {
+            "state_rel_diff": float(np.abs(u[z["cells"]] - z["states"]).max() / np.abs(z["states"]).max()),
+            "cl_cdp_rel_diff": [float(abs(fun[k] - z["functionals"][k]) / abs(z["functionals"][k])) for k in (0, 1)]}
+    cpu = f"{platform.machine()}, {nthreads} threads"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": 1, "warmup": 0, "ms_per_step": solve_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded NACA 0012 O-grid, the oracle's own generator; freestream start)",
+            "config": workload_config(world, args.small),
+            "solve": solve,
+            "note": f"one complete solve timed whole (it takes minutes); the requested --steps {args.steps} "
+                    f"--warmup {args.warmup} are not repeated",
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                             "sample": f"one complete solve of the workload on the oracle ({cpu}; natural-order "
+                                       f"ILU(0) as PETSc's): {st1['steps']} + {st2['steps']} steps, "
+                                       f"{st1['lin_iters']} + {st2['lin_iters']} Krylov iterations"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------- kernel micro-benchmarks ------------------------
+
+def run_kernel(args):
+    """Profiling aid: R launches of one kernel family, mean time per launch
+    (CUDA events) after three untimed launches."""
+    import torch
+
+    import fvens_gb300 as fv
+    from fvens_gb300 import build as fvbuild
     if not os.path.exists(fv.LIB_PATH):
         fvbuild.build_library()
-    m = fv.UMesh.generate(fv.MESH_NACA_OGRID, MESH, reorder=1)
-    vals = []
-    for k in range(args.warmup + args.steps):
-        cb = cpu_baseline(m, {"steps": STARTER["max_timesteps"], "lin_iters": args.ref_starter_iters},
-                          {"steps": args.ref_steps_per_solve, "lin_iters": args.ref_iters_per_solve},
-                          args.cpu_seconds / max(args.steps + args.warmup, 1))
-        if k >= args.warmup:
-            vals.append(cb)
-    value = statistics.median([v["value"] for v in vals])
-    cb = dict(vals[-1])
-    cb["value"] = value
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NACA 0012 O-grid generator)",
-            "config": {"workload": WORKLOAD, "cells": m.nelem, "faces": m.naface},
-            "cpu_baseline": cb, "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+    dev = torch.device("cuda", 0)
+    R = args.reps
+    if args.kernel == "fp64peak":
+        rate, ms = fv.fp64_peak(R)
+        print(f"fp64 peak: {rate / 1e9:.1f} G FMA/s = {2 * rate / 1e12:.4f} TFLOP/s (best launch {ms:.3f} ms)")
+        return
+    if args.kernel == "mpnn":
+        return _kernel_mpnn(fv, torch, dev, args.batch_members, R)
+    m, main, start = build_case(fv)
+    rng = np.random.default_rng(1234)
+    u = torch.tensor(np.tile(main.freestream()[0], (m.nelem, 1)) * (1 + 0.05 * rng.uniform(-1, 1, (m.nelem, 4))),
+                     device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    if args.kernel == "residual":
+        r = torch.zeros_like(u)
+        dt = torch.zeros(m.nelem, dtype=torch.float64, device=dev)
+        call = lambda: main.compute_residual(u, r, True, dt)
+        what = f"residual ({m.nelem} cells, {m.naface} faces)"
+    else:
+        A = fv.BlockMatrix(start, 4)
+        if args.kernel == "jacobian":
+            call = lambda: start.assemble_jacobian(u, A)
+            what = f"FP32 first-order Jacobian ({m.nelem} cells)"
+        else:
+            start.assemble_jacobian(u, A)
+            A.add_diagonal(torch.tensor(m.geometry()["area"] / 0.01, device=dev))  # pseudo-time term
+            P = fv.Preconditioner(start, A, "ilu0", part_size=args.part)
+            P.setup()
+            x = torch.tensor(rng.normal(size=(m.nelem, 4)), device=dev)
+            z = torch.zeros_like(x)
+            call = lambda: P.apply(x, z)
+            what = f"FP32 ILU(0) apply ({m.nelem} cells, parts of <= {args.part})"
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    a, b = ev(), ev()
+    a.record()
+    for _ in range(R):
+        call()
+    b.record()
+    torch.cuda.synchronize()
+    print(f"{what}: {a.elapsed_time(b) / R:.4f} ms per launch sequence")
+
+
+def _kernel_mpnn(fv, torch, dev, B, steps):
+    from fvens_gb300.mpnn import MPNN
+    m, _ = _laminar_mesh(fv, 0)
+    phs = _laminar_conditions(fv, B, 11)
+    net = MPNN(m, layers=4, wall_markers=(2,), seed=11)
+    net.set_scale(np.array([0.05, 0.1, 0.1, 0.2], np.float32))
+    tgt = torch.empty((B * m.nelem, 4), dtype=torch.float64, device=dev)
+    net.predict(phs, tgt)
+    tgt *= 1.01
+    for _ in range(3):
+        net.train_step(phs, tgt, 1e-4)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        net.train_step(phs, tgt, 1e-4)
+    b.record()
+    torch.cuda.synchronize()
+    t_train = a.elapsed_time(b) / steps
+    u = torch.empty_like(tgt)
+    a.record()
+    for _ in range(steps):
+        net.predict(phs, u)
+    b.record()
+    torch.cuda.synchronize()
+    print(f"mpnn: train step {t_train:.3f} ms, predict {a.elapsed_time(b) / steps:.3f} ms, "
+          f"{B} conditions x {m.nelem} cells")
 
 
 def main():
@@ -670,35 +963,41 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--kernel", choices=["residual", "ilu", "jacobian", "mpnn", "fp64peak"],
+                    help="profiling aid: time one kernel family instead of the benchmark")
+    ap.add_argument("--reps", type=int, default=5, help="launches timed by --kernel")
+    ap.add_argument("--part", type=int, default=128, help="--kernel ilu: cells per part of the block-colour order")
+    ap.add_argument("--batch-members", type=int, default=16, help="--kernel mpnn: conditions per training step")
+    ap.add_argument("--small", action="store_true",
+                    help="a 64 x 32 O-grid of the workload's family (CPU tests of the launch path; named so in "
+                         "config.workload)")
     ap.add_argument("--plain", action="store_true", help="FP64 Jacobian and preconditioner (the plain path)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nvtx", action="store_true", help="profiling aid: NVTX range around each main solve")
-    ap.add_argument("--no-variants", action="store_true",
-                    help="skip the plain-FP64 and warm-start comparison solves")
+    ap.add_argument("--no-variants", action="store_true", help="skip every comparison variant")
     ap.add_argument("--no-graph", action="store_true",
                     help="profiling aid: issue every launch from the host instead of replaying a CUDA graph")
-    ap.add_argument("--max-main-steps", type=int, default=0,
-                    help="profiling aid: cap the main solve's pseudo-time steps (the solve then does not converge)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--ref-steps-per-solve", type=int, default=1100,
-                    help="main-solve pseudo-time steps per solve assumed by the reference arm")
-    ap.add_argument("--ref-iters-per-solve", type=int, default=26000,
-                    help="main-solve Krylov iterations per solve assumed by the reference arm")
-    ap.add_argument("--ref-starter-iters", type=int, default=1800,
-                    help="starter Krylov iterations per solve assumed by the reference arm")
-    ap.add_argument("--warm-train", type=int, default=512,
-                    help="training conditions of the learned warm-start variant (0 skips it; 2048 for the full set)")
+    ap.add_argument("--e2e-solves", type=int, default=5, help="solves timed end to end through host buffers")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the batched laminar and warm-start variants")
+    ap.add_argument("--laminar-levels", type=int, default=2,
+                    help="refinements of the reference's 13,156-cell hybrid mesh for the laminar variants")
+    ap.add_argument("--batch", type=int, default=64, help="conditions per batched laminar solve")
+    ap.add_argument("--warm-train", type=int, default=128,
+                    help="training conditions of the learned warm-start variant (0 skips it)")
     ap.add_argument("--warm-test", type=int, default=64, help="held-out conditions of the warm-start variant")
     ap.add_argument("--warm-epochs", type=int, default=60, help="training epochs of the warm-start network")
-    ap.add_argument("--no-large", dest="large", action="store_false",
-                    help="skip the ~4M-cell kernel-throughput variant")
+    ap.add_argument("--no-large", dest="large", action="store_false", help="skip the ~4M-cell variant")
+    ap.add_argument("--no-large-solve", dest="large_solve", action="store_false",
+                    help="~4M-cell variant: kernel times only, no end-to-end solves")
     args = ap.parse_args()
-    if args.max_main_steps > 0:
-        MAIN["max_timesteps"] = args.max_main_steps
     if args.no_graph:
         STARTER["use_graph"] = 0
         MAIN["use_graph"] = 0
-    if args.impl == "reference":
+    if args.kernel:
+        run_kernel(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -377,6 +377,14 @@ def kernel_launch_count():
     return int(lib().fv_kernel_launch_count())
 
 
+def fp64_peak(reps=5):
+    """FP64 throughput ceiling of the current device: (FMA thread-instructions
+    per second, best launch in ms) from fv_fp64_peak."""
+    rate, ms = ctypes.c_double(), ctypes.c_double()
+    check(lib().fv_fp64_peak(int(reps), ctypes.byref(rate), ctypes.byref(ms)))
+    return rate.value, ms.value
+
+
 class Preconditioner:
     """PETSc PC equivalent on a BlockMatrix: 'jacobi', 'sgs' or 'ilu0'."""
 

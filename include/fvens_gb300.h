@@ -314,6 +314,13 @@ long long fv_solver_kernels_per_step(const fv_solver *s);
 #define FV_KERNEL_PRECOND_SETUP 5   /* factorisation */
 #define FV_KERNEL_GRADIENTS 6       /* residual passes before the face kernel (states, gradients, limiter) */
 fv_status fv_solver_time_kernel(fv_solver *s, const double *d_u, int which, int reps, double *avg_ms, double *bytes);
+/* FP64 throughput ceiling of the current device (a measurement aid; no
+ * counterpart in the reference): a kernel of independent FP64 fused
+ * multiply-add chains on every SM, timed with CUDA events, best of reps
+ * launches after one warm-up.  *h_dfma_per_s = FMA thread-instructions per
+ * second (2 FLOP each); *h_best_ms (may be NULL) = the best launch's time.
+ * Changes no clock or power setting.  Synchronises. */
+fv_status fv_fp64_peak(int reps, double *h_dfma_per_s, double *h_best_ms);
 
 /* ---- explicit time stepping ---- */
 /* SteadyForwardEulerSolver::solve (aodesolver.cpp:136-282): d_u (device,

@@ -71,7 +71,7 @@ def test_reference_arm_under_torchrun_prints_once():
     env = dict(os.environ, OMP_NUM_THREADS="2")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-seconds", "2"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--small"]
     out = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [x for x in out.stdout.splitlines() if x.startswith("{")]
@@ -79,6 +79,11 @@ def test_reference_arm_under_torchrun_prints_once():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["value"] > 0 and line["n_gpus"] == 2
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+    # one complete solve timed whole, on the oracle's own mesh (same workload description as the GPU arm)
+    assert line["steps"] == 1 and line["solve"]["main_steps"] > 0
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.workload_config(2, small=True)
 
 
 def test_bench_cpu_baseline_on_small_naca_mesh():
@@ -91,7 +96,8 @@ def test_bench_cpu_baseline_on_small_naca_mesh():
     m = fv.UMesh.generate(fv.MESH_NACA_OGRID, [64, 32, 30.0, 0, 0, 1.1, 12, 3], reorder=1)
     _, od2 = bench._oracle_case(m)
     u = np.tile(od2.freestream(), (m.nelem, 1))
-    cb = bench.cpu_baseline(m, {"steps": 10, "lin_iters": 50}, {"steps": 20, "lin_iters": 200}, 1.0, u)
+    cb = bench.cpu_baseline(m, 1.0, u, counts={"starter": {"steps": 10, "lin_iters": 50},
+                                              "main": {"steps": 20, "lin_iters": 200}})
     assert cb["unit"] == "solves/s" and cb["kind"] == "port" and cb["value"] > 0 and cb["cores"] >= 1
     assert "10 + 20 steps" in cb["sample"]
     assert set(cb["kernels_ms"]) == {"residual", "jacobian", "ilu0_setup", "ilu0_apply"}
