@@ -74,3 +74,44 @@ def _refine_once(mesh):
     new_bface = np.stack([np.stack([bface[:, 0], bm], 1), np.stack([bm, bface[:, 1]], 1)], 1).reshape(-1, 2)
     return dict(coords=new_coords, nnode=new_nnode.astype(np.int32), inpoel=out.reshape(-1, 4).astype(np.int32),
                 bface=new_bface.astype(np.int32), btag=np.repeat(btag, 2).astype(np.int32))
+
+
+def _progression(length, npoints, ratio):
+    """npoints positions from 0 to length whose successive spacings grow by
+    `ratio` (Gmsh's "Using Progression")."""
+    seg = ratio ** np.arange(npoints - 1, dtype=np.float64)
+    return length * np.concatenate([[0.0], np.cumsum(seg)]) / seg.sum()
+
+
+def flat_plate_stretched(levels=0):
+    """The structured laminar flat-plate mesh of the reference's
+    testcases/visc-flatplate/grids/flatplatestructstretched.geo (refinement
+    factor 2), refined `levels` times as its RefineMesh steps do (levels 0, 1,
+    2 are flatplatestructstretched0/1/2.msh).  Domain [-0.5, 1] x [0, 1] in
+    two transfinite blocks of quadrilaterals: ahead of the plate 10 points in
+    x with spacing growing by 1.2 away from the leading edge, on the plate 20
+    points growing by 1.1 from it, 20 points in y growing by 1.4 from the
+    wall.  Markers: 2 the plate (0 <= x <= 1, y = 0), 3 the symmetry line
+    ahead of it, 4 the inflow and top sides, 5 the outflow side (x = 1)."""
+    ref = 2
+    nxi, nxp, ny = 5 * ref, 10 * ref, 10 * ref
+    xs = np.concatenate([-_progression(0.5, nxi, 1.2)[::-1], _progression(1.0, nxp, 1.1)[1:]])
+    ys = _progression(1.0, ny, 1.4)
+    nx = len(xs)
+    X, Y = np.meshgrid(xs, ys)
+    coords = np.stack([X.ravel(), Y.ravel()], 1)
+    node = lambda i, j: j * nx + i
+    I, J = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1))
+    I, J = I.ravel(), J.ravel()
+    inpoel = np.stack([node(I, J), node(I + 1, J), node(I + 1, J + 1), node(I, J + 1)], 1)
+    i = np.arange(nx - 1)
+    j = np.arange(ny - 1)
+    bface = np.concatenate([np.stack([node(i, 0), node(i + 1, 0)], 1),
+                            np.stack([node(nx - 1, j), node(nx - 1, j + 1)], 1),
+                            np.stack([node(i + 1, ny - 1), node(i, ny - 1)], 1),
+                            np.stack([node(0, j + 1), node(0, j)], 1)])
+    btag = np.concatenate([np.where(xs[1:] <= 0.0, 3, 2), np.full(ny - 1, 5), np.full(nx - 1, 4),
+                           np.full(ny - 1, 4)])
+    mesh = dict(coords=coords, nnode=np.full(len(inpoel), 4, np.int32), inpoel=inpoel.astype(np.int32),
+                bface=bface.astype(np.int32), btag=btag.astype(np.int32))
+    return refine(mesh, levels)

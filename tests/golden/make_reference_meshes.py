@@ -7,6 +7,8 @@ Reads, with this project's own Gmsh 2.2 reader (cells kept in file order):
   testcases/naca0012/grids/naca0012luo.msh                 -> naca0012luo_mesh.npz
   testcases/visc-naca0012/grids/NACA0012_lam_hybrid_1.msh  -> naca0012_lam_hybrid_1_mesh.npz
   testcases/2dcylinder/grids/2dcylinder{0..3}.msh           -> 2dcylinder_meshes.npz
+and the exact lift and drag of the laminar flat plate,
+  tests/visc-flatplate/exact_clcd_flatplate.dat            -> flatplate_exact_clcd.npz
 The functional-regression values the tests compare with are the reference's
 files testcases/naca0012/regr-MUSCL_LeastSquares_HLLC.txt and
 testcases/visc-naca0012/regr-LeastSquares_Roe.txt, stored alongside; the
@@ -37,6 +39,10 @@ def _arrays(e, prefix=""):
 
 
 def main(root):
+    with open(os.path.join(root, "tests/visc-flatplate/exact_clcd_flatplate.dat")) as f:
+        exact = [float(x) for x in f.read().split()[:3]]
+    np.savez_compressed(os.path.join(HERE, "flatplate_exact_clcd.npz"), exact=np.array(exact))
+    print("flat plate exact CL, CDp, CDsf", exact)
     cyl = {}
     for k in range(4):
         m = fv.UMesh.read_gmsh(os.path.join(root, f"testcases/2dcylinder/grids/2dcylinder{k}.msh"), reorder=0)

@@ -73,3 +73,40 @@ def load_cylinders():
 # 15000 steps) and main solve (CFL 0.25, relative 1e-4, 60000 steps)
 CYLINDER_EXPLICIT = dict(flux="ROE", gradient="GREENGAUSS", start=dict(cfl=0.5, tolerance=1e-1, max_timesteps=15000),
                          main=dict(cfl=0.25, tolerance=1e-4, max_timesteps=60000), nmesh=3)
+
+
+# The reference's laminar flat-plate skin-friction convergence test
+# (tests/visc-flatplate: flatplate.ctrl, flatplate.solverc; CTest
+# SpatialFlow_NS_FlatPlate_LeastSquares_Roe_Struct_CDConvergence, driver
+# tests/flow_clcd_conv.cpp) on flatplatestructstretched0..2 (fvens_gb300.meshes
+# .flat_plate_stretched): M 0.2, Re 8.7e5, T 290.19 K, Pr 0.708, Sutherland
+# viscosity; Roe, least squares, no limiter; starter CFL 20-2000, relative
+# 1e-1, 50 steps; main CFL 100-4000, relative 1e-5, 500 steps; robust_flow
+# update; -pc_type ilu, -mesh_reorder rcm.  Passes when the order of the
+# skin-friction drag error between the two finest meshes lies in [0.95, 1.5].
+FLAT_PLATE = dict(
+    bcs=[(3, "slipwall", ()), (4, "farfield", ()), (5, "inflowoutflow", ()), (2, "adiabaticwall", (0.0,))],
+    phys=dict(Minf=0.2, aoa_deg=0.0, Reinf=8.7e5, Tinf=290.19, Pr=0.708, viscous=True),
+    flux="ROE", gradient="LEASTSQUARES",
+    start_solver=dict(cfl_min=20, cfl_max=2000, tolerance=1e-1, max_timesteps=50),
+    main_solver=dict(cfl_min=100, cfl_max=4000, tolerance=1e-5, max_timesteps=500),
+    pc="ilu0", nl_update="robust_flow", nmesh=3, band=(0.95, 1.5))
+
+
+def load_flat_plates():
+    """flatplatestructstretched0..2 (RCM-ordered) and the reference's exact
+    (CL, CDp, CDsf) of tests/visc-flatplate/exact_clcd_flatplate.dat."""
+    from fvens_gb300 import meshes
+    out = []
+    for lv in range(FLAT_PLATE["nmesh"]):
+        a = meshes.flat_plate_stretched(lv)
+        out.append(fv.UMesh.from_arrays(a["coords"], a["nnode"], a["inpoel"], a["bface"], a["btag"], reorder=1))
+    return out, np.load(os.path.join(GOLDEN, "flatplate_exact_clcd.npz"))["exact"]
+
+
+def flat_plate_order(meshes_, cdsf, exact):
+    """flow_clcd_conv.cpp's order of the skin-friction drag error between the
+    last two meshes: h = 1/sqrt(cells) (casesolvers.cpp:96)."""
+    lh = [np.log10(1.0 / np.sqrt(m.nelem)) for m in meshes_]
+    le = [np.log10(abs(abs(c) - exact[2])) for c in cdsf]
+    return (le[-1] - le[-2]) / (lh[-1] - lh[-2])

@@ -129,3 +129,40 @@ def test_entropy_errors_on_reference_cylinders_match_oracle(cuda):
         logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(e)))
     slope = (logs[1][1] - logs[0][1]) / (logs[1][0] - logs[0][0])
     assert 1.65 <= slope <= 2.1, (slope, logs)
+
+
+def test_flat_plate_skin_friction_matches_oracle_and_converges(cuda):
+    """The reference's laminar flat-plate skin-friction convergence test on
+    the GPU (FP32-preconditioned path), with the starter of its control file
+    and the main solve driven to an absolute 1e-10: on every mesh the
+    converged state and CDsf agree with the oracle's converged solve within
+    1e-8, and the order of the CDsf error between the two finest meshes lies
+    in the reference's band [0.95, 1.5]."""
+    import torch
+
+    from tests.test_regression_cpu import _flat_plate_oracle
+    c = rc.FLAT_PLATE
+    meshes_, exact = rc.load_flat_plates()
+    cdsf = []
+    for m in meshes_:
+        ph = fv.physics_cfg(**c["phys"])
+        start = fv.FlowFV(m, ph, fv.numerics_cfg(flux=c["flux"], gradient="NONE"), c["bcs"])
+        main = fv.FlowFV(m, ph, fv.numerics_cfg(flux=c["flux"], gradient=c["gradient"]), c["bcs"])
+        ud = torch.tensor(np.tile(main.freestream()[0], (m.nelem, 1)), device=cuda)
+        s1, s2 = c["start_solver"], c["main_solver"]
+        fv.SteadyBackwardEulerSolver(start, cfl_min=s1["cfl_min"], cfl_max=s1["cfl_max"], tolerance=s1["tolerance"],
+                                     abs_tolerance=0, max_timesteps=s1["max_timesteps"], pc=c["pc"],
+                                     nl_update=c["nl_update"], precision=4).solve(ud, raise_on_error=False)
+        _, st = fv.SteadyBackwardEulerSolver(main, cfl_min=s2["cfl_min"], cfl_max=s2["cfl_max"], tolerance=1e-10,
+                                             abs_tolerance=1, max_timesteps=3000, pc=c["pc"],
+                                             nl_update=c["nl_update"], precision=4).solve(ud)
+        assert st[0]["status"] == 0 and st[0]["res"] <= 1e-10
+        f = main.surface_data(ud, 2)[0]
+        uo, sto, fo = _flat_plate_oracle(m, 1e-10, True, 3000)
+        assert sto["status"] == 0
+        ug = ud.cpu().numpy()
+        assert np.abs(ug - uo).max() <= 1e-8 * np.abs(uo).max()
+        assert abs(f[2] - fo[2]) <= 1e-8 * abs(fo[2])
+        cdsf.append(f[2])
+    order = rc.flat_plate_order(meshes_, cdsf, exact)
+    assert c["band"][0] <= order <= c["band"][1], (order, cdsf)

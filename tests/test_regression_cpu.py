@@ -96,3 +96,35 @@ def test_oracle_explicit_entropy_convergence_on_reference_cylinders():
         logs.append((np.log10(1.0 / np.sqrt(m.nelem)), np.log10(d2.entropy_error(u2))))
     slope = (logs[-1][1] - logs[-2][1]) / (logs[-1][0] - logs[-2][0])
     assert 1.65 <= slope <= 2.1, (slope, logs)
+
+
+def _flat_plate_oracle(m, tol, abs_tol, maxiter):
+    c = rc.FLAT_PLATE
+    om = orc.Mesh.from_export(m.export())
+    d1 = orc.Disc(om, **c["phys"], flux=c["flux"], gradient="NONE", bcs=c["bcs"])
+    d2 = orc.Disc(om, **c["phys"], flux=c["flux"], gradient=c["gradient"], bcs=c["bcs"])
+    s1 = c["start_solver"]
+    u1, _ = d1.steady_solve(np.tile(d2.freestream(), (m.nelem, 1)), cflmin=s1["cfl_min"], cflmax=s1["cfl_max"],
+                            tol=s1["tolerance"], maxiter=s1["max_timesteps"], abs_tol=False, pc=c["pc"],
+                            nl_update=c["nl_update"])
+    s2 = c["main_solver"]
+    u2, st = d2.steady_solve(u1, cflmin=s2["cfl_min"], cflmax=s2["cfl_max"], tol=tol, maxiter=maxiter,
+                             abs_tol=abs_tol, pc=c["pc"], nl_update=c["nl_update"])
+    return u2, st, d2.surface_data(u2, 2)
+
+
+def test_oracle_flat_plate_skin_friction_convergence():
+    """The reference's SpatialFlow_NS_FlatPlate_LeastSquares_Roe_Struct_CDConvergence
+    (tests/flow_clcd_conv.cpp with tests/visc-flatplate/flatplate.ctrl and
+    flatplate.solverc) on flatplatestructstretched0..2: the order of the
+    skin-friction drag error against exact_clcd_flatplate.dat between the two
+    finest meshes lies in [0.95, 1.5]."""
+    c = rc.FLAT_PLATE
+    meshes_, exact = rc.load_flat_plates()
+    cdsf = []
+    for m in meshes_:
+        _, st, f = _flat_plate_oracle(m, c["main_solver"]["tolerance"], False, c["main_solver"]["max_timesteps"])
+        assert st["status"] in (0, 6), st["status"]   # a step-limited solve is kept, as run_output does
+        cdsf.append(f[2])
+    order = rc.flat_plate_order(meshes_, cdsf, exact)
+    assert c["band"][0] <= order <= c["band"][1], (order, cdsf)
