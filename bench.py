@@ -53,8 +53,11 @@ NUM_START = dict(flux="HLLC", gradient="NONE")
 BCS = [(2, "slipwall", ()), (4, "farfield", ())]
 STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
                min_relax=0.2, pc="ilu0")
+# FGMRES relative tolerance 0.3 (PETSc's -ksp_rtol; the reference's control files
+# use 0.1): with 0.1 the solve's path is sensitive enough to rounding that it
+# stalls just above 1e-10 for some perturbations of the matrix-free step
 MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
-            min_relax=0.2, pc="ilu0", matrix_free=1)
+            min_relax=0.2, pc="ilu0", matrix_free=1, ksp_rtol=0.3)
 WORKLOAD = "naca0012_transonic_512x256_ogrid_g1.02_hllc_gg_venkat5"
 METRIC = "solves/s to ||R||<1e-10 (transonic NACA0012, matrix-free FGMRES, FP32 Jacobian + FP32 block-colour ILU0)"
 C2_FIXTURE = os.path.join(ROOT, "tests", "golden", "naca0012_transonic_oracle_converged.npz")
@@ -368,11 +371,14 @@ def run_variants(fv, torch, dev, m, main, start, u0d, prec, args):
     if args.large:
         out["large_4m"] = run_large(fv, torch, dev, float(_peaks().get("hbm_gbs", 6800.0)), args.large_solve)
     if args.batched:
-        out["batched_laminar"] = bl = run_batched(fv, torch, dev, args.laminar_levels, args.batch)
-        if args.warm_train > 0:
+        bl, tr_phys, tr_u = run_batched(fv, torch, dev, args.laminar_levels, args.batch, sgs=args.laminar_sgs)
+        out["batched_laminar"] = bl
+        if args.warm_test > 0 and (args.warm_train > 0 or tr_phys):
             out["warm_start_laminar"] = run_warm_start(
                 fv, torch, dev, args.laminar_levels, args.warm_train, args.warm_test, args.warm_epochs, args.batch,
-                plain_single_s=bl["single_plain_fp64"]["seconds"])
+                plain_single_s=bl["single_plain_fp64"]["seconds"],
+                train=None if args.warm_train > 0 else (tr_phys, tr_u))
+        del tr_u
     return out
 
 
@@ -448,46 +454,57 @@ def _vs_laminar_fixture(m, levels, main, u, members):
     return out
 
 
-def run_batched(fv, torch, dev, levels=2, B=64, seed=7):
+def run_batched(fv, torch, dev, levels=2, B=64, seed=7, sgs=False):
     """Batched solves of B laminar conditions (M ~ U[0.3, 0.7], AoA ~ U[-4, 4] deg,
     Re ~ U[2000, 10000], Pr 0.72, adiabatic wall; Roe, least squares) on the
     reference's hybrid NACA 0012 mesh refined `levels` times, all members in
-    the same launches with FP32 Jacobians and block SGS (and with ILU(0)),
-    against member 0 alone on the FP32 path and on the plain FP64 path."""
+    the same launches with FP32 Jacobians and ILU(0) (with sgs, also with
+    block SGS), against member 0 alone on the FP32 path and on the plain FP64
+    path.  Returns (results, conditions and device states of the batch's
+    converged members)."""
     import collections
     m, nlines = _laminar_mesh(fv, levels)
     phs = _laminar_conditions(fv, B, seed)
-    res = {"mesh_cells": m.nelem, "mesh_faces": m.naface, "refinements": levels, "batch": B, "lines": nlines}
-    for tag, plist, prec, pc in (("single_plain_fp64", phs[:1], 8, "ilu0"), ("single", phs[:1], 4, "ilu0"),
-                                 ("batch_sgs", phs, 4, "sgs"), ("batch", phs, 4, "ilu0")):
+    res = {"mesh_cells": m.nelem, "mesh_faces": m.naface, "refinements": levels, "batch": B, "lines": nlines,
+           "max_main_steps": LAMINAR_MAIN["max_timesteps"]}
+    runs = [("single_plain_fp64", phs[:1], 8, "ilu0"), ("single", phs[:1], 4, "ilu0"), ("batch", phs, 4, "ilu0")]
+    if sgs:
+        runs.append(("batch_sgs", phs, 4, "sgs"))
+    conv_phys, conv_states = [], None
+    for tag, plist, prec, pc in runs:
         main, solvers = _laminar_solvers(fv, m, plist, prec, pc=pc)
         u = _freestream_field(torch, dev, main, m.nelem)
         t, stats = _timed_solve(torch, solvers, u, all_members=True)
-        conv = sum(1 for st in stats if st["status"] == 0)
-        res[tag] = {"seconds": t, "converged": conv, "members": len(plist), "converged_solves_s": conv / t,
+        conv = [k for k, st in enumerate(stats) if st["status"] == 0]
+        res[tag] = {"seconds": t, "converged": len(conv), "members": len(plist), "converged_solves_s": len(conv) / t,
                     "status_counts": dict(collections.Counter(int(st["status"]) for st in stats)),
                     "main_steps_max": max(st["steps"] for st in stats),
                     "main_steps_mean": float(np.mean([st["steps"] for st in stats])),
+                    "main_steps_mean_converged": float(np.mean([stats[k]["steps"] for k in conv])) if conv else None,
                     "linear_iters_mean": float(np.mean([st["lin_iters"] for st in stats]))}
         if tag in ("single_plain_fp64", "batch"):
-            res[tag]["vs_oracle"] = _vs_laminar_fixture(m, levels, main, u,
-                                                        [k for k, st in enumerate(stats) if st["status"] == 0])
+            res[tag]["vs_oracle"] = _vs_laminar_fixture(m, levels, main, u, conv)
+        if tag == "batch" and conv:
+            conv_phys = [plist[k] for k in conv]
+            conv_states = u.view(len(plist), m.nelem, 4)[torch.as_tensor(conv, device=u.device)].clone()
         del main, solvers, u
-    best = max(res["batch"]["converged_solves_s"], res["batch_sgs"]["converged_solves_s"])
+    best = max(res[k]["converged_solves_s"] for k in ("batch", "batch_sgs") if k in res)
     res["batch_vs_single_plain_fp64"] = best / max(res["single_plain_fp64"]["converged_solves_s"], 1e-30)
-    return res
+    return res, conv_phys, conv_states
 
 
-def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_single_s=None):
+def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_single_s=None, train=None):
     """Learned warm start on the laminar hybrid NACA 0012 case.
 
-    n_train conditions (seed 11) are solved in batches of B from freestream
-    (starter + main); the converged members train the message-passing network
-    (4 layers, width 64; BF16 tensor-core GEMMs, FP32 accumulation, Adam) on
-    the GPU.  n_test held-out conditions (seed 12, same distributions) are then
-    solved twice in batches of B on the FP32-preconditioned path: from
-    freestream with the starter, and from the network's prediction without it
-    (members that do not converge fall back to freestream).  Reported:
+    Training data: the converged members of a batched solve, given as
+    train = (conditions, device states), or else n_train conditions (seed 11)
+    solved here in batches of B from freestream (starter + main).  They train
+    the message-passing network (4 layers, width 64; BF16 tensor-core GEMMs,
+    FP32 accumulation, Adam) on the GPU.  n_test held-out conditions (seed
+    12, same distributions) are then solved twice in batches of at most B on
+    the FP32-preconditioned path: from freestream with the starter, and from
+    the network's prediction without it (members that do not converge fall
+    back to freestream).  Reported:
     nonlinear steps, wall time (CUDA events), initial-state error relative to
     the converged state, the largest difference of the two converged states
     and of their Cl/Cd, and the warm-started batch's rate against one plain
@@ -500,6 +517,9 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
     phs_te = _laminar_conditions(fv, n_test, 12)
     ev = lambda: torch.cuda.Event(enable_timing=True)
     keep_phys, keep_u, gen_s = [], [], 0.0
+    if train is not None:
+        keep_phys, keep_u = list(train[0]), list(train[1])
+        n_train = 0
     for s in range(0, n_train, B):
         plist = phs_tr[s:s + B]
         main, solvers = _laminar_solvers(fv, m, plist, 4)
@@ -524,7 +544,8 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
     torch.cuda.synchronize()
     train_s = a.elapsed_time(b) / 1e3
     del targets, keep_u
-    out = {"mesh_cells": m.nelem, "train_conditions": n_train, "train_converged": len(keep_phys),
+    out = {"mesh_cells": m.nelem, "train_conditions": n_train if train is None else "the batched variant's members",
+           "train_converged": len(keep_phys),
            "test_conditions": n_test, "epochs": epochs, "train_batch": 16, "params": net.nparams,
            "data_generation_s": gen_s, "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
     agg = {k: dict(seconds=0.0, steps=[], res0=[], status=collections.Counter()) for k in ("freestream", "warm")}
@@ -668,7 +689,8 @@ def run_large(fv, torch, dev, peak_gbs, solve=True):
             t, st = _timed_solve(torch, [S1, S2], u)
             cl = main.surface_data(u, 2)[0]
             out[tag] = {"solve_s": t, "main_steps": st["steps"], "linear_iters": st["lin_iters"],
-                        "status": st["status"], "res": st["res"], "cl_cdp_cdsf": [float(x) for x in cl]}
+                        "status": st["status"], "res0": st["res0"], "res": st["res"],
+                        "max_main_steps": LARGE_MAIN["max_timesteps"], "cl_cdp_cdsf": [float(x) for x in cl]}
             del S1, S2
         a, b = out["solve_fp32_precond"], out["solve_plain_fp64"]
         if a["status"] == 0 and b["status"] == 0:
@@ -678,7 +700,7 @@ def run_large(fv, torch, dev, peak_gbs, solve=True):
 
 LARGE_STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
                      min_relax=0.2, pc="ilu0")
-LARGE_MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=1500, nl_update=2,
+LARGE_MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=300, nl_update=2,
                   min_relax=0.2, pc="ilu0", matrix_free=1)
 
 
@@ -698,19 +720,22 @@ def _oracle_case(m):
     return od1, od2
 
 
-def oracle_solve(od1, od2, u):
+def oracle_solve(od1, od2, u, order=None):
     """One complete solve of the workload on the oracle: the starter and the
-    main solve with the workload's settings, natural-order ILU(0) as PETSc's.
+    main solve with the workload's settings, ILU(0) in the elimination order
+    `order` (cell at each position; None: natural order, as PETSc's).
     Returns (u, starter stats, main stats, starter seconds, main seconds)."""
     S, M = STARTER, MAIN
     t0 = time.perf_counter()
     u, st1 = od1.steady_solve(u, cflmin=S["cfl_min"], cflmax=S["cfl_max"], tol=S["tolerance"],
                               maxiter=S["max_timesteps"], abs_tol=bool(S["abs_tolerance"]), pc="ilu0",
-                              nl_update="bounded", min_relax=S["min_relax"])
+                              nl_update="bounded", min_relax=S["min_relax"], lin_rtol=S.get("ksp_rtol", 0.1),
+                              order=order)
     t1 = time.perf_counter()
     u, st2 = od2.steady_solve(u, cflmin=M["cfl_min"], cflmax=M["cfl_max"], tol=M["tolerance"],
                               maxiter=M["max_timesteps"], abs_tol=bool(M["abs_tolerance"]), pc="ilu0",
-                              nl_update="bounded", min_relax=M["min_relax"], matrix_free=bool(M["matrix_free"]))
+                              nl_update="bounded", min_relax=M["min_relax"], matrix_free=bool(M["matrix_free"]),
+                              lin_rtol=M.get("ksp_rtol", 0.1), order=order)
     t2 = time.perf_counter()
     return u, st1, st2, t1 - t0, t2 - t1
 
@@ -761,6 +786,7 @@ def oracle_parity(m, main, ud):
     u_conv = ud.detach().cpu().numpy().reshape(m.nelem, 4)
     rng = np.random.default_rng(1234)
     u_pert = np.tile(od2.freestream(), (m.nelem, 1)) * (1 + 0.05 * rng.uniform(-1, 1, (m.nelem, 4)))
+    area = m.geometry()["area"]
     for tag, u in (("converged", u_conv), ("perturbed", u_pert)):
         udev = torch.tensor(u, device=ud.device)
         r = torch.zeros_like(udev)
@@ -768,6 +794,10 @@ def oracle_parity(m, main, ud):
         main.synchronize()
         ro, _ = od2.residual(u)
         out[f"residual_{tag}_max_rel_err"] = float(np.abs(r.cpu().numpy() - ro).max() / od2.flux_scale(u).max())
+        if tag == "converged":
+            # the solver's norm (area-weighted energy residual) of the oracle's
+            # residual at the GPU's converged state
+            out["oracle_residual_norm_at_gpu_state"] = float(np.sqrt(np.sum(ro[:, 3] ** 2 * area)))
     cg = main.surface_data(ud, 2)[0]
     co = od2.surface_data(u_conv, 2)
     out["cl_cdp_rel_err"] = [float(abs(cg[k] - co[k]) / abs(co[k])) for k in (0, 1)]
@@ -844,13 +874,20 @@ def run_reference(args):
     om, od1, od2 = _oracle_case_from_arrays(arrs)
     t_mesh = time.perf_counter() - t0
     u = np.tile(od2.freestream(), (om.nelem, 1))
-    u, st1, st2, ts, tm = oracle_solve(od1, od2, u)
+    # ILU(0) in the GPU's block-colour elimination order, stored with the
+    # committed fixture (PETSc's natural order diverges on this workload)
+    order, order_note = None, "natural order (as PETSc's)"
+    if os.path.exists(C2_FIXTURE) and not args.small:
+        order = np.load(C2_FIXTURE)["order"]
+        order_note = "the GPU's block-colour elimination order (parts of <= 128 cells)"
+    u, st1, st2, ts, tm = oracle_solve(od1, od2, u, order)
     solve_s = ts + tm
     value = 1.0 / solve_s
     fun = od2.surface_data(u, 2)
     solve = {"starter_steps": st1["steps"], "starter_linear_iters": st1["lin_iters"], "main_steps": st2["steps"],
              "linear_iters": st2["lin_iters"], "converged": st2["status"] == 0, "final_res": float(st2["res"]),
-             "cl_cdp": [float(fun[0]), float(fun[1])], "starter_s": ts, "main_s": tm, "mesh_setup_s": t_mesh}
+             "cl_cdp": [float(fun[0]), float(fun[1])], "starter_s": ts, "main_s": tm, "mesh_setup_s": t_mesh,
+             "ilu0_order": order_note}
     if os.path.exists(C2_FIXTURE) and not args.small:
         z = np.load(C2_FIXTURE)
         solve["vs_committed_oracle_solve"] = {
@@ -866,8 +903,8 @@ def run_reference(args):
             "note": f"one complete solve timed whole (it takes minutes); the requested --steps {args.steps} "
                     f"--warmup {args.warmup} are not repeated",
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
-                             "sample": f"one complete solve of the workload on the oracle ({cpu}; natural-order "
-                                       f"ILU(0) as PETSc's): {st1['steps']} + {st2['steps']} steps, "
+                             "sample": f"one complete solve of the workload on the oracle ({cpu}; ILU(0) in "
+                                       f"{order_note}): {st1['steps']} + {st2['steps']} steps, "
                                        f"{st1['lin_iters']} + {st2['lin_iters']} Krylov iterations"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -984,14 +1021,20 @@ def main():
     ap.add_argument("--laminar-levels", type=int, default=2,
                     help="refinements of the reference's 13,156-cell hybrid mesh for the laminar variants")
     ap.add_argument("--batch", type=int, default=64, help="conditions per batched laminar solve")
-    ap.add_argument("--warm-train", type=int, default=128,
-                    help="training conditions of the learned warm-start variant (0 skips it)")
-    ap.add_argument("--warm-test", type=int, default=64, help="held-out conditions of the warm-start variant")
+    ap.add_argument("--laminar-sgs", action="store_true", help="batched laminar variant: also block SGS")
+    ap.add_argument("--warm-train", type=int, default=0,
+                    help="training conditions of the learned warm-start variant, solved for it (0: train on the "
+                         "batched variant's converged members)")
+    ap.add_argument("--warm-test", type=int, default=16,
+                    help="held-out conditions of the warm-start variant (0 skips it)")
     ap.add_argument("--warm-epochs", type=int, default=60, help="training epochs of the warm-start network")
     ap.add_argument("--no-large", dest="large", action="store_false", help="skip the ~4M-cell variant")
     ap.add_argument("--no-large-solve", dest="large_solve", action="store_false",
                     help="~4M-cell variant: kernel times only, no end-to-end solves")
+    ap.add_argument("--large-steps", type=int, default=300,
+                    help="~4M-cell variant: main-solve step limit of the end-to-end solves")
     args = ap.parse_args()
+    LARGE_MAIN["max_timesteps"] = args.large_steps
     if args.no_graph:
         STARTER["use_graph"] = 0
         MAIN["use_graph"] = 0

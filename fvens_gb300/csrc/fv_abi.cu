@@ -447,8 +447,9 @@ fv_status fv_disc_create(fv_mesh *m, const fv_physics_cfg *phys, int batch, cons
 	// per-face / per-cell precomputation
 	const int ne = h.nelem, nf = h.naface, nb = h.nbface;
 	const DiscArrays da = disc_arrays(h, num->reconstruction == FV_REC_VENKATAKRISHNAN, num->limiter_param);
-	const std::vector<double2> &fwdr = da.fwdr, &fggw = da.fggw;
-	const std::vector<d4> &fvis = da.fvis, &vinv = da.vinv;
+	const bool ls = num->gradientscheme == FV_GRAD_LEASTSQUARES;
+	const std::vector<d4> &gcoef = ls ? da.gcoef_ls : da.gcoef_gg;
+	const std::vector<d4> &fvis = da.fvis;
 	const std::vector<double> &veps2 = da.veps2;
 	DiscDev &d = D->d;
 	std::memset(&d, 0, sizeof(d));
@@ -464,25 +465,23 @@ fv_status fv_disc_create(fv_mesh *m, const fv_physics_cfg *phys, int batch, cons
 	d.limparam = num->limiter_param;
 	cudaError_t e = cudaSuccess;
 	std::vector<void *> *own = &D->owned;
-	int *bcid_d; BCDev *bcs_d; Phys *phys_d; double2 *fwdr_d, *fggw_d; d4 *fvis_d, *vinv_d; double *veps_d;
+	int *bcid_d; BCDev *bcs_d; Phys *phys_d; d4 *gcoef_d, *fvis_d; double2 *gself_d; double *veps_d;
 	if (!e) e = dupload(&bcid_d, bcid, own);
 	if (!e) e = dupload(&bcs_d, D->bcs_h.empty() ? std::vector<BCDev>(1, BCDev{0, 0, 0}) : D->bcs_h, own);
 	if (!e) e = dupload(&phys_d, D->phys_h, own);
-	if (!e) e = dupload(&fwdr_d, fwdr, own);
-	if (!e) e = dupload(&fggw_d, fggw, own);
+	if (!e) e = dupload(&gcoef_d, gcoef, own);
+	if (!e) e = dupload(&gself_d, da.gself_gg, own);
 	if (!e) e = dupload(&fvis_d, fvis, own);
-	if (!e) e = dupload(&vinv_d, vinv, own);
 	if (!e) e = dupload(&veps_d, veps2, own);
-	d.bcid = bcid_d; d.bcs = bcs_d; d.phys = phys_d; d.fwdr = fwdr_d; d.fggw = fggw_d; d.fvis = fvis_d;
-	d.vinv = vinv_d; d.veps2 = veps_d;
+	d.bcid = bcid_d; d.bcs = bcs_d; d.phys = phys_d; d.gcoef = gcoef_d; d.gself = gself_d; d.fvis = fvis_d;
+	d.veps2 = veps_d;
 	ResidualWork &w = D->w;
 	const size_t B = batch;
 	if (!e) e = dalloc(&w.prim, B * ne, own);
 	if (!e) e = dalloc(&w.ghost_prim, B * std::max(nb, 1), own);
 	if (!e) e = dalloc(&w.ghost_cons, B * std::max(nb, 1), own);
 	if (!e) e = dalloc(&w.grad, 2 * B * ne, own);
-	if (!e) e = dalloc(&w.lgrad, num->reconstruction == FV_REC_WENO ? 2 * B * ne : 1, own);
-	if (!e) e = dalloc(&w.phi, B * ne, own);
+	if (!e) e = dalloc(&w.lgrad, recon_gradients(num->reconstruction) ? 2 * B * ne : 1, own);
 	if (!e) e = dalloc(&w.fflux, B * nf, own);
 	if (!e) e = dalloc(&w.spec, B * nf, own);
 	if (!e) e = dupload(&D->btag, nb > 0 ? h.btag : std::vector<int>(1, 0), own);

@@ -67,11 +67,14 @@ struct DiscDev {
 	const int *bcid;                // per boundary face: index into bcs
 	const BCDev *bcs;
 	const Phys *phys;               // [batch]
-	// precomputed per-face data
-	const double2 *fwdr;            // WLS: w2 * (rc_L - rc_R) (R = ghost centre on boundary)
-	const double2 *fggw;            // GG: (dL, dR)/(dL + dR) * len
+	// precomputed gradient coefficients per cell and local edge j (the
+	// gradient is linear in the cell's and its neighbours' values):
+	//   Green-Gauss  grad_i = gself_i q_i + sum_j gcoef_ij q_nbr(j)
+	//   least squares grad_i = sum_j gcoef_ij (q_nbr(j) - q_i)
+	// gcoef[2 i] = (x, y of edge 0, x, y of edge 1), gcoef[2 i + 1] = edges 2, 3
+	const d4 *gcoef;
+	const double2 *gself;           // Green-Gauss self coefficient (x, y)
 	const d4 *fvis;                 // viscous: unit (rc_R - rc_L), 1/|rc_R - rc_L|
-	const d4 *vinv;                 // WLS inverse 2x2 per cell (a, b, c, d)
 	const double *veps2;            // Venkatakrishnan (K h)^3 per cell
 	// configuration
 	int flux, jflux, gradscheme, recon, order2, viscous, constvisc;
@@ -83,14 +86,17 @@ struct DiscDev {
 
 __device__ __forceinline__ bool skip_member(const DiscDev &D, int b) { return D.active && !D.active[b]; }
 
+/* reconstructions whose face values use gradients of their own (ResidualWork::lgrad) */
+inline bool recon_gradients(int recon) { return recon == 2 || recon == 3 || recon == 4; }
+
 /* Scratch of one residual evaluation (per batch member slices). */
 struct ResidualWork {
 	d4 *prim = nullptr;        // [batch][nelem]
 	d4 *ghost_prim = nullptr;  // [batch][nbface]  cell-centred ghost state, primitive
 	d4 *ghost_cons = nullptr;  // [batch][nbface]  cell-centred ghost state, conserved
 	d4 *grad = nullptr;        // [batch][nelem][2]
-	d4 *lgrad = nullptr;       // [batch][nelem][2] WENO-blended gradients
-	d4 *phi = nullptr;         // [batch][nelem] limiter values
+	d4 *lgrad = nullptr;       // [batch][nelem][2] reconstruction gradients: WENO-blended, or
+	                           // scaled by the Barth-Jespersen / Venkatakrishnan limiter values
 	d4 *fflux = nullptr;       // [batch][naface] integrated face fluxes
 	double2 *spec = nullptr;   // [batch][naface] spectral radii (left, right)
 };

@@ -419,6 +419,12 @@ FV_HD void flux_hll(const PP &P, const St<T> &L, const St<T> &Rr, const double *
 	for (int i = 0; i < 4; i++) f[i] = t1 * fj[i] + t2 * fi[i] - t3 * (ur[i] - ul[i]);
 }
 
+/* HLLC (anumericalflux.cpp:1040-1110).  Of its four cases (supersonic left,
+ * left star state, right star state, supersonic right) the left two use the
+ * left state and speed, the right two the right ones, with the same formulas:
+ * the side is picked by selection and one flux (plus, inside the fan, its
+ * star-state correction) is evaluated, so faces on either side of the
+ * contact take one path through the FP64 pipe instead of two. */
 template <class T, class PP>
 FV_HD void flux_hllc(const PP &P, const St<T> &L, const St<T> &Rr, const double *n, T *f)
 {
@@ -427,39 +433,26 @@ FV_HD void flux_hllc(const PP &P, const St<T> &L, const St<T> &Rr, const double 
 	einfeldt(P, L, Rr, n, vni, vnj, sl, sr);
 	const T sm = (Rr.r * vnj * (sr - vnj) - L.r * vni * (sl - vni) + L.p - Rr.p) /
 	             (Rr.r * (sr - vnj) - L.r * (sl - vni));
-	if (sl > R(0)) {
-		dir_flux(L, vni, n, f);
-	} else if (sm > R(0)) {
-		// F_L + sl (U*_L - U_L), star state anumericalflux.cpp:1071-1081
-		dir_flux(L, vni, n, f);
-		const T a = sl - vni, is = R(1) / (sl - sm);
-		const T dps = L.r * (vni - sl) * (vni - sm);  // p* - p
-		T ul[4];
-		st_cons(L, ul);
-		const T us0 = L.r * a * is;
-		const T us1 = (a * ul[1] + dps * R(n[0])) * is;
-		const T us2 = (a * ul[2] + dps * R(n[1])) * is;
-		const T us3 = (a * L.E - L.p * vni + (dps + L.p) * sm) * is;
-		f[0] = f[0] + sl * (us0 - ul[0]);
-		f[1] = f[1] + sl * (us1 - ul[1]);
-		f[2] = f[2] + sl * (us2 - ul[2]);
-		f[3] = f[3] + sl * (us3 - ul[3]);
-	} else if (sr >= R(0)) {
-		dir_flux(Rr, vnj, n, f);
-		const T a = sr - vnj, is = R(1) / (sr - sm);
-		const T dps = Rr.r * (vnj - sr) * (vnj - sm);
-		T ur[4];
-		st_cons(Rr, ur);
-		const T us0 = Rr.r * a * is;
-		const T us1 = (a * ur[1] + dps * R(n[0])) * is;
-		const T us2 = (a * ur[2] + dps * R(n[1])) * is;
-		const T us3 = (a * Rr.E - Rr.p * vnj + (dps + Rr.p) * sm) * is;
-		f[0] = f[0] + sr * (us0 - ur[0]);
-		f[1] = f[1] + sr * (us1 - ur[1]);
-		f[2] = f[2] + sr * (us2 - ur[2]);
-		f[3] = f[3] + sr * (us3 - ur[3]);
-	} else {
-		dir_flux(Rr, vnj, n, f);
+	const bool left = sl > R(0) || sm > R(0);
+	const bool star = left ? !(sl > R(0)) : (sr >= R(0));
+	const St<T> &S = left ? L : Rr;
+	const T vn = left ? vni : vnj;
+	const T sk = left ? sl : sr;
+	dir_flux(S, vn, n, f);
+	if (star) {
+		// F_K + s_K (U*_K - U_K), star state anumericalflux.cpp:1071-1081
+		const T a = sk - vn, is = R(1) / (sk - sm);
+		const T dps = S.r * (vn - sk) * (vn - sm);  // p* - p
+		T uk[4];
+		st_cons(S, uk);
+		const T us0 = S.r * a * is;
+		const T us1 = (a * uk[1] + dps * R(n[0])) * is;
+		const T us2 = (a * uk[2] + dps * R(n[1])) * is;
+		const T us3 = (a * S.E - S.p * vn + (dps + S.p) * sm) * is;
+		f[0] = f[0] + sk * (us0 - uk[0]);
+		f[1] = f[1] + sk * (us1 - uk[1]);
+		f[2] = f[2] + sk * (us2 - uk[2]);
+		f[3] = f[3] + sk * (us3 - uk[3]);
 	}
 }
 

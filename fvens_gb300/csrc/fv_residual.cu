@@ -9,8 +9,8 @@
 //   face fluxes            flow_spatial.cpp:488-563, anumericalflux.cpp
 //   viscous flux           flow_spatial.cpp:348-395, aspatial.cpp:172-205, viscousphysics.cpp:15-122
 //   local time steps       flow_spatial.cpp:565-634
-// Structure: five launches per evaluation (prep, gradient+limiter, WENO blend,
-// face flux, cell gather).  Face fluxes are written once per face and gathered
+// Structure: up to five launches per evaluation (prep, gradient+limiter,
+// WENO blend, face flux, cell gather).  Face fluxes are written once per face and gathered
 // by cells in a fixed order, so results are deterministic and need no atomics.
 #include "fv_residual_body.cuh"
 
@@ -68,13 +68,13 @@ __global__ void __launch_bounds__(kMaxBS) k_prep_mf(DiscDev D, const double *__r
 }
 
 __global__ void __launch_bounds__(kMaxBS) k_grad(DiscDev D, const d4 *__restrict__ q, const d4 *__restrict__ qg,
-                                                 d4 *__restrict__ grad, d4 *__restrict__ phi, int limiter)
+                                                 d4 *__restrict__ grad, d4 *__restrict__ lgrad, int limiter)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= D.nelem) return;
-	grad_body(D, b, i, q, qg, grad, phi, limiter);
+	grad_body(D, b, i, q, qg, grad, lgrad, limiter);
 }
 
 __global__ void __launch_bounds__(kMaxBS) k_weno(DiscDev D, const d4 *__restrict__ grad, d4 *__restrict__ lgrad)
@@ -185,20 +185,16 @@ cudaError_t gradient_pass_launch(fv_disc_impl *Dh, const double *u, cudaStream_t
 	nk++;
 	if (D.gradscheme != GRAD_NONE) {
 		const int lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
-		k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.prim, W.ghost_prim, W.grad, W.phi, lim);
+		k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.prim, W.ghost_prim, W.grad, W.lgrad, lim);
 		nk++;
 		if (D.recon == REC_WENO) {
 			k_weno<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.grad, W.lgrad);
 			nk++;
 		}
 	} else {
+		// no gradients: every face value equals the cell value
 		cudaMemsetAsync(W.grad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
-		if (D.recon == REC_WENO) cudaMemsetAsync(W.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
-		if (D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN) {
-			// zero gradients: every face value equals the cell value, the limiter is 1
-			k_grad<<<grid_of(D.nelem, bg, B), bg, 0, s>>>(D, W.prim, W.ghost_prim, W.grad, W.phi, 0);
-			nk++;
-		}
+		if (recon_gradients(D.recon)) cudaMemsetAsync(W.lgrad, 0, sizeof(d4) * 2 * (size_t)D.nelem * B, s);
 	}
 	Dh->kernels_launched += nk;
 	return cudaGetLastError();
@@ -256,7 +252,7 @@ cudaError_t gradients_launch(fv_disc_impl *Dh, const double *u, double *grad, in
 		cudaMemsetAsync(grad, 0, sizeof(double) * 8 * (size_t)D.nelem * B, s);
 		Dh->kernels_launched += 1;
 	} else {
-		k_grad<<<grid(D.nelem), BS, 0, s>>>(D, q, qg, reinterpret_cast<d4 *>(grad), Dh->w.phi, 0);
+		k_grad<<<grid(D.nelem), BS, 0, s>>>(D, q, qg, reinterpret_cast<d4 *>(grad), Dh->w.lgrad, 0);
 		Dh->kernels_launched += 2;
 	}
 	return cudaGetLastError();
@@ -288,7 +284,7 @@ cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s,
 		case KBS_PREP: k_prep<<<grid_of(D.nelem + D.nbface, bs, B), bs, 0, s>>>(D, u, Dh->w); break;
 		case KBS_GRAD:
 			if (D.order2) k_grad<<<grid_of(D.nelem, bs, B), bs, 0, s>>>(D, Dh->w.prim, Dh->w.ghost_prim, Dh->w.grad,
-			                                                              Dh->w.phi, lim);
+			                                                              Dh->w.lgrad, lim);
 			break;
 		case KBS_FACE: Dh->bs[KBS_FACE] = bs; face_launch(Dh, u, 1, s); break;
 		default: k_gather<<<grid_of(D.nelem, bs, B), bs, 0, s>>>(D, Dh->w, r, nullptr); break;

@@ -1,6 +1,8 @@
 // Per-cell / per-face bodies of the residual evaluation (host/device), used
 // by the kernels in fv_residual.cu; see that file for the reference mapping.
 #pragma once
+#include <cstring>
+
 #include "fv_core.cuh"
 
 namespace fvg {
@@ -47,12 +49,32 @@ FV_HD void prep_body(const DiscDev &D, int b, int t, const double *__restrict__ 
 	}
 }
 
-/* 2. cell gradients (Green-Gauss or weighted least squares), gathered over
- *    the cell's faces; optionally the Barth-Jespersen / Venkatakrishnan limiter
- *    of the cell (its neighbour values and face centres are already at hand).
+/* 64-bit integer that orders like the double x (for non-NaN x): its bit
+ * pattern with the magnitude bits of negative values flipped, so that the
+ * limiter's comparisons run on the integer pipes and leave the FP64 pipe,
+ * which bounds these kernels, to the arithmetic. */
+FV_HD long long order_key(double x)
+{
+#ifdef __CUDA_ARCH__
+	const long long b = __double_as_longlong(x);
+#else
+	long long b;
+	std::memcpy(&b, &x, sizeof b);
+#endif
+	return b >= 0 ? b : b ^ 0x7fffffffffffffffLL;
+}
+
+/* sign bit of x (true for negative values and -0) */
+FV_HD bool sign_bit(double x) { return order_key(x) < 0; }
+
+/* 2. cell gradients (Green-Gauss or weighted least squares) from the cell's
+ *    and its neighbours' values with precomputed per-cell coefficients
+ *    (DiscDev::gcoef); optionally the Barth-Jespersen / Venkatakrishnan
+ *    limiter of the cell, whose limited gradients (the limiter value times
+ *    the gradient, per variable) go to lgrad for the face reconstruction.
  *    q: cell states [batch][nelem], qg: ghost states [batch][nbface]. */
 FV_HD void grad_body(const DiscDev &D, int b, int i, const d4 *__restrict__ q, const d4 *__restrict__ qg,
-                     d4 *__restrict__ grad, d4 *__restrict__ phi, int limiter)
+                     d4 *__restrict__ grad, d4 *__restrict__ lgrad, int limiter)
 {
 	const d4 *qb = q + (size_t)b * D.nelem;
 	const d4 *qgb = qg + (size_t)b * D.nbface;
@@ -60,43 +82,48 @@ FV_HD void grad_body(const DiscDev &D, int b, int i, const d4 *__restrict__ q, c
 	const int4 cf = D.cface[i], cn = D.cnbr[i];
 	const int fl[4] = {cf.x, cf.y, cf.z, cf.w};
 	const int nbr[4] = {cn.x, cn.y, cn.z, cn.w};
+	const d4 c01 = D.gcoef[2 * (size_t)i], c23 = D.gcoef[2 * (size_t)i + 1];
+	const double cx[4] = {c01.x, c01.z, c23.x, c23.z}, cy[4] = {c01.y, c01.w, c23.y, c23.w};
 	d4 qn[4];
-	double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 	for (int j = 0; j < 4; j++) {
-		if (fl[j] < 0) { qn[j] = qi; continue; }
-		const int f = fl[j] >> 1, side = fl[j] & 1;
 		const int nb = nbr[j];
-		qn[j] = nb >= 0 ? qb[nb] : qgb[-1 - nb];
-		if (D.gradscheme == GRAD_LEASTSQUARES) {
-			const double2 wd = D.fwdr[f];
-			for (int v = 0; v < 4; v++) {
-				const double dq = side ? comp(qn[j], v) - comp(qi, v) : comp(qi, v) - comp(qn[j], v);
-				acc[2 * v] += wd.x * dq;
-				acc[2 * v + 1] += wd.y * dq;
-			}
-		} else {
-			const double2 ww = D.fggw[f];
-			const d4 g = D.fgeo[f];
-			const double s = side ? -1.0 : 1.0;
-			for (int v = 0; v < 4; v++) {
-				const double qL = side ? comp(qn[j], v) : comp(qi, v);
-				const double qR = side ? comp(qi, v) : comp(qn[j], v);
-				const double ut = (qL * ww.x + qR * ww.y) * s;
-				acc[2 * v] += ut * g.x;
-				acc[2 * v + 1] += ut * g.y;
-			}
-		}
+		qn[j] = fl[j] < 0 ? qi : (nb >= 0 ? qb[nb] : qgb[-1 - nb]);
 	}
 	double gr[8];
 	if (D.gradscheme == GRAD_LEASTSQUARES) {
-		const d4 V = D.vinv[i];
+		// sum_j V^-1 w2 dr_ij (q_j - q_i)   (agradientschemes.cpp:219-317)
+#pragma unroll
 		for (int v = 0; v < 4; v++) {
-			gr[2 * v] = V.x * acc[2 * v] + V.y * acc[2 * v + 1];
-			gr[2 * v + 1] = V.z * acc[2 * v] + V.w * acc[2 * v + 1];
+			const double uv = comp(qi, v);
+			double gx = 0, gy = 0;
+#pragma unroll
+			for (int j = 0; j < 4; j++) {
+				if (fl[j] < 0) continue;
+				const double d = comp(qn[j], v) - uv;
+				gx = fma(cx[j], d, gx);
+				gy = fma(cy[j], d, gy);
+			}
+			gr[2 * v] = gx;
+			gr[2 * v + 1] = gy;
 		}
 	} else {
-		const double ia = D.iarea[i];
-		for (int k = 0; k < 8; k++) gr[k] = acc[k] * ia;
+		// (sum over faces of the weighted face value x normal x length) / area
+		// (agradientschemes.cpp:62-216), split into the cell's and the neighbours' terms
+		const double2 sc = D.gself[i];
+#pragma unroll
+		for (int v = 0; v < 4; v++) {
+			const double uv = comp(qi, v);
+			double gx = sc.x * uv, gy = sc.y * uv;
+#pragma unroll
+			for (int j = 0; j < 4; j++) {
+				if (fl[j] < 0) continue;
+				const double qv = comp(qn[j], v);
+				gx = fma(cx[j], qv, gx);
+				gy = fma(cy[j], qv, gy);
+			}
+			gr[2 * v] = gx;
+			gr[2 * v + 1] = gy;
+		}
 	}
 	d4 *gb = grad + 2 * ((size_t)b * D.nelem + i);
 	gb[0] = d4{gr[0], gr[1], gr[2], gr[3]};
@@ -114,40 +141,50 @@ FV_HD void grad_body(const DiscDev &D, int b, int i, const d4 *__restrict__ q, c
 		dx[j] = fc.x - ci.x;
 		dy[j] = fc.y - ci.y;
 	}
-	d4 lim;
+	double lg[8];
+#pragma unroll
 	for (int v = 0; v < 4; v++) {
 		const double uv = comp(qi, v);
+		// largest and smallest neighbour difference, each with 0
 		double dmin = 0, dmax = 0;
+		long long kmin = 0, kmax = 0;
+#pragma unroll
 		for (int j = 0; j < 4; j++) {
 			if (fl[j] < 0) continue;
 			const double d = comp(qn[j], v) - uv;
-			if (d > dmax) dmax = d;
-			if (d < dmin) dmin = d;
+			const long long k = order_key(d);
+			if (k > kmax) { kmax = k; dmax = d; }
+			if (k < kmin) { kmin = k; dmin = d; }
 		}
 		// the smallest of 1 and the faces' ratios num/den (den > 0), found by
 		// comparing cross products so that only the winner is divided
 		double bn = 1.0, bd = 1.0;
+#pragma unroll
 		for (int j = 0; j < 4; j++) {
 			if (fl[j] < 0) continue;
-			double uf = uv;
-			uf += 1.0 * gr[2 * v] * dx[j];
-			uf += 1.0 * gr[2 * v + 1] * dy[j];
-			const double dm = uf - uv;
+			// unlimited increment to the face centre
+			const double dm = fma(gr[2 * v], dx[j], gr[2 * v + 1] * dy[j]);
+			const bool neg = sign_bit(dm);
 			double num, den;
 			if (venkat) {
-				const double dp = dm < 0 ? dmin : dmax;
-				num = dp * dp + 2 * dp * dm + eps2;
-				den = dp * dp + dp * dm + 2 * dm * dm + eps2;
+				const double dp = neg ? dmin : dmax;
+				const double t2 = dm + dm;
+				num = fma(dp, dp + t2, eps2);                // dp^2 + 2 dp dm + eps^2
+				den = fma(dp, dp + dm, fma(t2, dm, eps2));   // dp^2 + dp dm + 2 dm^2 + eps^2
 			} else {
-				if (dm == 0) continue;  // ratio 1
-				num = dm > 0 ? dmax : -dmin;
-				den = dm > 0 ? dm : -dm;
+				if ((order_key(dm) & 0x7fffffffffffffffLL) == 0) continue;  // dm = 0: ratio 1
+				num = neg ? -dmin : dmax;
+				den = fabs(dm);
 			}
-			if (num * bd < bn * den) { bn = num; bd = den; }
+			if (sign_bit(fma(num, bd, -(bn * den)))) { bn = num; bd = den; }
 		}
-		setc(lim, v, bn == bd ? 1.0 : bn / bd);
+		const double phi = bn == bd ? 1.0 : bn / bd;
+		lg[2 * v] = phi * gr[2 * v];
+		lg[2 * v + 1] = phi * gr[2 * v + 1];
 	}
-	phi[(size_t)b * D.nelem + i] = lim;
+	d4 *lb = lgrad + 2 * ((size_t)b * D.nelem + i);
+	lb[0] = d4{lg[0], lg[1], lg[2], lg[3]};
+	lb[1] = d4{lg[4], lg[5], lg[6], lg[7]};
 }
 
 /* 3. WENO-blended gradients (limitedlinearreconstruction.cpp:40-80):
@@ -272,31 +309,18 @@ FV_HD void face_body(const DiscDev &D, int b, int f, const double *__restrict__ 
 				}
 			}
 		} else {
-			const d4 *gsrc = D.recon == REC_WENO ? w.lgrad : w.grad;
-			const bool lim = D.recon == REC_BARTHJESPERSEN || D.recon == REC_VENKATAKRISHNAN;
+			// linear reconstruction with the cell gradients, WENO-blended or
+			// already scaled by the limiter values (grad_body)
+			const d4 *gsrc = D.recon == REC_NONE ? w.grad : w.lgrad;
 			double gl[8];
 			load_grad(gsrc, cb + L, gl);
-			const d4 pL = lim ? w.phi[cb + L] : d4{1, 1, 1, 1};
 			const double dxl = fc.x - cL.x, dyl = fc.y - cL.y;
-			for (int v = 0; v < 4; v++) {
-				const double l = comp(pL, v);
-				double x = comp(qL, v);
-				x += l * gl[2 * v] * dxl;
-				x += l * gl[2 * v + 1] * dyl;
-				qfL[v] = x;
-			}
+			for (int v = 0; v < 4; v++) qfL[v] = fma(gl[2 * v + 1], dyl, fma(gl[2 * v], dxl, comp(qL, v)));
 			if (!bnd) {
 				double gr[8];
 				load_grad(gsrc, cb + Rc, gr);
-				const d4 pR = lim ? w.phi[cb + Rc] : d4{1, 1, 1, 1};
 				const double dxr = fc.x - cR.x, dyr = fc.y - cR.y;
-				for (int v = 0; v < 4; v++) {
-					const double l = comp(pR, v);
-					double x = comp(qR, v);
-					x += l * gr[2 * v] * dxr;
-					x += l * gr[2 * v + 1] * dyr;
-					qfR[v] = x;
-				}
+				for (int v = 0; v < 4; v++) qfR[v] = fma(gr[2 * v + 1], dyr, fma(gr[2 * v], dxr, comp(qR, v)));
 			}
 		}
 		sL = st_from_prim(P, qfL);

@@ -53,18 +53,21 @@ inline MeshArrays mesh_arrays(const HostMesh &h)
 }
 
 struct DiscArrays {
-	std::vector<double2> fwdr, fggw;
-	std::vector<d4> fvis, vinv;
+	std::vector<d4> gcoef_gg, gcoef_ls;  // [nelem][2] (see DiscDev::gcoef)
+	std::vector<double2> gself_gg;
+	std::vector<d4> fvis;
 	std::vector<double> veps2;
 };
 
-/* Per-face gradient weights and viscous geometry, per-cell WLS inverses and
- * Venkatakrishnan thresholds. */
+/* Per-cell gradient coefficients (Green-Gauss and weighted least squares),
+ * per-face viscous geometry and per-cell Venkatakrishnan thresholds. */
 inline DiscArrays disc_arrays(const HostMesh &h, bool venkat, double limparam)
 {
 	DiscArrays a;
 	const int ne = h.nelem, nf = h.naface, nb = h.nbface;
-	a.fwdr.resize(nf); a.fggw.resize(nf); a.fvis.resize(nf); a.vinv.resize(ne); a.veps2.assign(ne, 0.0);
+	std::vector<double2> fwdr(nf), fggw(nf);
+	std::vector<d4> vinv(ne);
+	a.fvis.resize(nf); a.veps2.assign(ne, 0.0);
 	std::vector<double> V(4 * (size_t)ne, 0.0);
 	for (int f = 0; f < nf; f++) {
 		const int L = h.face_l[f];
@@ -74,7 +77,7 @@ inline DiscArrays disc_arrays(const HostMesh &h, bool venkat, double limparam)
 		// weighted least squares (agradientschemes.cpp:219-317)
 		const double dx = xl - xr, dy = yl - yr;
 		const double w2 = 1.0 / (dx * dx + dy * dy);
-		a.fwdr[f] = make_double2(w2 * dx, w2 * dy);
+		fwdr[f] = make_double2(w2 * dx, w2 * dy);
 		const double va = w2 * dx * dx, vb = w2 * dx * dy, vc = w2 * dy * dy;
 		V[4 * L] += va; V[4 * L + 1] += vb; V[4 * L + 2] += vb; V[4 * L + 3] += vc;
 		if (f >= nb) {
@@ -86,7 +89,7 @@ inline DiscArrays disc_arrays(const HostMesh &h, bool venkat, double limparam)
 		const double dL = 1.0 / std::sqrt((mx - xl) * (mx - xl) + (my - yl) * (my - yl));
 		const double dR = 1.0 / std::sqrt((mx - xr) * (mx - xr) + (my - yr) * (my - yr));
 		const double len = h.fnorm[3 * f + 2];
-		a.fggw[f] = make_double2(dL / (dL + dR) * len, dR / (dL + dR) * len);
+		fggw[f] = make_double2(dL / (dL + dR) * len, dR / (dL + dR) * len);
 		// viscous face geometry (aspatial.cpp:172-205)
 		const double ex = xr - xl, ey = yr - yl, dist = std::sqrt(ex * ex + ey * ey);
 		a.fvis[f] = d4{ex / dist, ey / dist, 1.0 / dist, dist};
@@ -94,7 +97,40 @@ inline DiscArrays disc_arrays(const HostMesh &h, bool venkat, double limparam)
 	for (int i = 0; i < ne; i++) {
 		const double va = V[4 * i], vb = V[4 * i + 1], vc = V[4 * i + 2], vd = V[4 * i + 3];
 		const double det = va * vd - vb * vc;
-		a.vinv[i] = d4{vd / det, -vb / det, -vc / det, va / det};
+		vinv[i] = d4{vd / det, -vb / det, -vc / det, va / det};
+	}
+	// Per cell and local edge j: the coefficients of the neighbour's value.
+	// Green-Gauss (agradientschemes.cpp:62-216): sum over faces of the
+	// inverse-distance-weighted face value times the face normal and length,
+	// over the area; the cell's own value collects the weights of its side.
+	// Weighted least squares (agradientschemes.cpp:219-317): V^-1 w2 dr_ij
+	// multiplying (q_j - q_i), dr_ij the neighbour's centre minus the cell's.
+	a.gcoef_gg.assign(2 * (size_t)ne, d4{0, 0, 0, 0});
+	a.gcoef_ls.assign(2 * (size_t)ne, d4{0, 0, 0, 0});
+	a.gself_gg.assign(ne, make_double2(0, 0));
+	for (int i = 0; i < ne; i++) {
+		const double ia = 1.0 / h.area[i];
+		const d4 Vi = vinv[i];
+		double sx = 0, sy = 0, gg[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ls[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+		for (int j = 0; j < h.nnode[i] && j < 4; j++) {
+			const int f = h.elemface[4 * i + j];
+			const bool left = h.face_l[f] == i;
+			const double nx = h.fnorm[3 * f], ny = h.fnorm[3 * f + 1];
+			// the cell's weight and the neighbour's, signed for the outward normal
+			const double wself = left ? fggw[f].x : -fggw[f].y;
+			const double wnbr = left ? fggw[f].y : -fggw[f].x;
+			sx += wself * nx; sy += wself * ny;
+			gg[2 * j] = wnbr * nx * ia; gg[2 * j + 1] = wnbr * ny * ia;
+			// w2 (r_nbr - r_i): fwdr holds w2 (r_L - r_R)
+			const double ex = left ? -fwdr[f].x : fwdr[f].x, ey = left ? -fwdr[f].y : fwdr[f].y;
+			ls[2 * j] = Vi.x * ex + Vi.y * ey;
+			ls[2 * j + 1] = Vi.z * ex + Vi.w * ey;
+		}
+		a.gself_gg[i] = make_double2(sx * ia, sy * ia);
+		a.gcoef_gg[2 * i] = d4{gg[0], gg[1], gg[2], gg[3]};
+		a.gcoef_gg[2 * i + 1] = d4{gg[4], gg[5], gg[6], gg[7]};
+		a.gcoef_ls[2 * i] = d4{ls[0], ls[1], ls[2], ls[3]};
+		a.gcoef_ls[2 * i + 1] = d4{ls[4], ls[5], ls[6], ls[7]};
 	}
 	if (venkat) {
 		// characteristic length = longest cell edge (limitedlinearreconstruction.cpp:180-205)

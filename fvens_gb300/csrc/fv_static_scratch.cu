@@ -1,7 +1,7 @@
 /*
  * fv_compute_residual_static: the residual evaluation of fv_compute_residual
  * (same kernels, same results) with its scratch -- primitive and ghost
- * states, gradients, limiter values, face fluxes and face spectral radii --
+ * states, gradients, reconstruction gradients, face fluxes and face spectral radii --
  * carved out of one file-scope device array instead of the buffers the
  * discretisation handle allocated for itself.
  *
@@ -49,7 +49,7 @@ size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
 /* Lays the scratch of one evaluation out from base (NULL: sizes only);
  * returns the bytes used.  Sizes as the handle's own buffers (fv_disc_create). */
-size_t carve(const fvg::DiscDev &d, int batch, bool weno, unsigned char *base, fvg::ResidualWork *w)
+size_t carve(const fvg::DiscDev &d, int batch, bool lgrad, unsigned char *base, fvg::ResidualWork *w)
 {
 	const size_t B = batch, ne = d.nelem, nf = d.naface, nb = d.nbface > 0 ? d.nbface : 1;
 	size_t off = 0;
@@ -64,8 +64,7 @@ size_t carve(const fvg::DiscDev &d, int batch, bool weno, unsigned char *base, f
 	take(&x.ghost_prim, B * nb);
 	take(&x.ghost_cons, B * nb);
 	take(&x.grad, 2 * B * ne);
-	take(&x.lgrad, weno ? 2 * B * ne : 1);
-	take(&x.phi, B * ne);
+	take(&x.lgrad, lgrad ? 2 * B * ne : 1);
 	take(&x.fflux, B * nf);
 	take(&x.spec, B * nf);
 	return off;
@@ -78,8 +77,8 @@ using namespace fvg;
 extern "C" fv_status fv_compute_residual_static(fv_disc *D, const double *u, double *r, int gettimesteps, double *dt)
 {
 	if (!D || !u || !r || (gettimesteps && !dt)) { set_error("null argument"); return FV_ERR_INVALID; }
-	const bool weno = D->d.recon == FV_REC_WENO;
-	const size_t need = carve(D->d, D->batch, weno, nullptr, nullptr);
+	const bool lg = recon_gradients(D->d.recon);
+	const size_t need = carve(D->d, D->batch, lg, nullptr, nullptr);
 	if (need > kStaticScratchBytes) {
 		set_error("static residual scratch: this discretisation needs " + std::to_string(need) +
 		          " bytes (cells x batch too large); the static array holds " + std::to_string(kStaticScratchBytes));
@@ -105,7 +104,7 @@ extern "C" fv_status fv_compute_residual_static(fv_disc *D, const double *u, dou
 		base = g_scratch_addr[dev];
 	}
 	ResidualWork w;
-	carve(D->d, D->batch, weno, static_cast<unsigned char *>(base), &w);
+	carve(D->d, D->batch, lg, static_cast<unsigned char *>(base), &w);
 	const int before = D->kernels_launched;
 	e = residual_launch(D, u, r, gettimesteps, dt, D->stream, &w);
 	count_launches(D->kernels_launched - before);

@@ -134,10 +134,11 @@ def test_entropy_errors_on_reference_cylinders_match_oracle(cuda):
 def test_flat_plate_skin_friction_matches_oracle_and_converges(cuda):
     """The reference's laminar flat-plate skin-friction convergence test on
     the GPU (FP32-preconditioned path), with the starter of its control file
-    and the main solve driven to an absolute 1e-10: on every mesh the
-    converged state and CDsf agree with the oracle's converged solve within
-    1e-8, and the order of the CDsf error between the two finest meshes lies
-    in the reference's band [0.95, 1.5]."""
+    and the main solve driven to an absolute 1e-12 (at 1e-10 the skin
+    friction itself is converged to only ~6e-7): on every mesh the converged
+    state and CDsf agree with the oracle's converged solve within 1e-8, and
+    the order of the CDsf error between the two finest meshes lies in the
+    reference's band [0.95, 1.5]."""
     import torch
 
     from tests.test_regression_cpu import _flat_plate_oracle
@@ -153,12 +154,12 @@ def test_flat_plate_skin_friction_matches_oracle_and_converges(cuda):
         fv.SteadyBackwardEulerSolver(start, cfl_min=s1["cfl_min"], cfl_max=s1["cfl_max"], tolerance=s1["tolerance"],
                                      abs_tolerance=0, max_timesteps=s1["max_timesteps"], pc=c["pc"],
                                      nl_update=c["nl_update"], precision=4).solve(ud, raise_on_error=False)
-        _, st = fv.SteadyBackwardEulerSolver(main, cfl_min=s2["cfl_min"], cfl_max=s2["cfl_max"], tolerance=1e-10,
+        _, st = fv.SteadyBackwardEulerSolver(main, cfl_min=s2["cfl_min"], cfl_max=s2["cfl_max"], tolerance=1e-12,
                                              abs_tolerance=1, max_timesteps=3000, pc=c["pc"],
                                              nl_update=c["nl_update"], precision=4).solve(ud)
-        assert st[0]["status"] == 0 and st[0]["res"] <= 1e-10
+        assert st[0]["status"] == 0 and st[0]["res"] <= 1e-12
         f = main.surface_data(ud, 2)[0]
-        uo, sto, fo = _flat_plate_oracle(m, 1e-10, True, 3000)
+        uo, sto, fo = _flat_plate_oracle(m, 1e-12, True, 3000)
         assert sto["status"] == 0
         ug = ud.cpu().numpy()
         assert np.abs(ug - uo).max() <= 1e-8 * np.abs(uo).max()
