@@ -160,6 +160,21 @@ FV_HD St<T> st_from_prim(const PP &P, const T *up)
 	return s;
 }
 
+/* st_from_prim of two states with one division: 1/r_a and 1/r_b from
+ * 1/(r_a r_b) (densities are positive and far from over- or underflow). */
+template <class T, class PP>
+FV_HD void st_pair_from_prim(const PP &P, const T *ua, const T *ub, St<T> &a, St<T> &b)
+{
+	typedef typename Real<T>::type R;
+	const T t = R(1) / (ua[0] * ub[0]);
+	a.r = ua[0]; a.u = ua[1]; a.v = ua[2]; a.p = ua[3];
+	b.r = ub[0]; b.u = ub[1]; b.v = ub[2]; b.p = ub[3];
+	a.ir = ub[0] * t;
+	b.ir = ua[0] * t;
+	a.E = a.p * R(P.igm1) + R(0.5) * a.r * (a.u * a.u + a.v * a.v);
+	b.E = b.p * R(P.igm1) + R(0.5) * b.r * (b.u * b.u + b.v * b.v);
+}
+
 template <class T> FV_HD void st_cons(const St<T> &s, T *uc) { uc[0] = s.r; uc[1] = s.r * s.u; uc[2] = s.r * s.v; uc[3] = s.E; }
 
 template <class T, class PP> FV_HD T sound_speed(const PP &P, const St<T> &s)
@@ -431,17 +446,21 @@ FV_HD void flux_hllc(const PP &P, const St<T> &L, const St<T> &Rr, const double 
 	typedef typename Real<T>::type R;
 	T vni, vnj, sl, sr;
 	einfeldt(P, L, Rr, n, vni, vnj, sl, sr);
-	const T sm = (Rr.r * vnj * (sr - vnj) - L.r * vni * (sl - vni) + L.p - Rr.p) /
-	             (Rr.r * (sr - vnj) - L.r * (sl - vni));
-	const bool left = sl > R(0) || sm > R(0);
+	// contact speed sm = num / den; den > 0 (both of its terms are: sr > vnj, sl < vni)
+	const T num = Rr.r * vnj * (sr - vnj) - L.r * vni * (sl - vni) + L.p - Rr.p;
+	const T den = Rr.r * (sr - vnj) - L.r * (sl - vni);
+	const bool left = sl > R(0) || num > R(0);
 	const bool star = left ? !(sl > R(0)) : (sr >= R(0));
 	const St<T> &S = left ? L : Rr;
 	const T vn = left ? vni : vnj;
 	const T sk = left ? sl : sr;
 	dir_flux(S, vn, n, f);
 	if (star) {
-		// F_K + s_K (U*_K - U_K), star state anumericalflux.cpp:1071-1081
-		const T a = sk - vn, is = R(1) / (sk - sm);
+		// F_K + s_K (U*_K - U_K), star state anumericalflux.cpp:1071-1081;
+		// sm and 1/(s_K - sm) from one division: e = den (s_K - sm)
+		const T e = sk * den - num, t = R(1) / (den * e);
+		const T sm = num * e * t, is = den * den * t;
+		const T a = sk - vn;
 		const T dps = S.r * (vn - sk) * (vn - sm);  // p* - p
 		T uk[4];
 		st_cons(S, uk);

@@ -323,14 +323,14 @@ FV_HD void face_body(const DiscDev &D, int b, int f, const double *__restrict__ 
 				for (int v = 0; v < 4; v++) qfR[v] = fma(gr[2 * v + 1], dyr, fma(gr[2 * v], dxr, comp(qR, v)));
 			}
 		}
-		sL = st_from_prim(P, qfL);
 		if (bnd) {
+			sL = st_from_prim(P, qfL);
 			double ul[4], gs[4];
 			st_cons(sL, ul);
 			ghost_cons<double>(P, D.bcs[D.bcid[f]], ul, n, gs, false);
 			sR = st_from_cons(P, gs);
 		} else {
-			sR = st_from_prim(P, qfR);
+			st_pair_from_prim(P, qfL, qfR, sL, sR);
 		}
 	}
 	double F[4];

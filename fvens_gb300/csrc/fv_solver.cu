@@ -690,23 +690,38 @@ long long fv_solver_kernels_per_step(const fv_solver *S) { return S ? S->kernels
 
 namespace {
 
-/* compulsory-traffic models (bytes per launch, all batch members) */
+/* compulsory-traffic models (bytes per launch, all batch members): every
+ * array element a launch sequence reads or writes, once */
 double bytes_model(const fv_solver *S, int which)
 {
 	const fv_disc_impl *D = S->D;
 	const double Nc = D->d.nelem, Nf = D->d.naface, Nb = D->d.nbface, B = D->batch;
-	const bool lim = D->d.recon == FV_REC_BARTHJESPERSEN || D->d.recon == FV_REC_VENKATAKRISHNAN ||
-	                 D->d.recon == FV_REC_WENO;
+	const int rec = D->d.recon;
+	const bool lim = rec == FV_REC_BARTHJESPERSEN || rec == FV_REC_VENKATAKRISHNAN;
+	const bool gg = D->d.gradscheme == FV_GRAD_GREENGAUSS;
+	const bool visc = D->d.viscous;
 	const double w = S->A.prec;
 	const double nblk = Nc + 2 * (Nf - Nb);  // stored blocks
+	// states, gradients and limiter pass: u in, primitive state out and in,
+	// connectivity, gradient coefficients, gradients out (+ centroid, threshold,
+	// limited gradients out, face centres); boundary faces: geometry, ghost states
+	const double grad_b = (272 - (gg ? 0 : 16) + (lim ? 88 : 0) + (rec == FV_REC_WENO ? 64 : 0)) * Nc +
+	                      (lim ? 16 * Nf : 0) + 128 * Nb;
+	// face kernel: per cell primitive state, reconstruction gradient, centroid;
+	// per face left/right, normal and length, centre, flux and spectral radii out;
+	// boundary faces ghost state and centre; viscous: face geometry (+ the
+	// unlimited gradient when a limiter is active)
+	const double face_b = (112 + (visc && lim ? 64 : 0)) * Nc + (104 + (visc ? 32 : 0)) * Nf + 48 * Nb;
+	// gather: connectivity, area, residual in and out, time step out; face fluxes and radii in
+	const double gather_b = 96 * Nc + 48 * Nf;
 	switch (which) {
 	case FV_KERNEL_RESIDUAL:
-		if (!D->d.order2) return B * (80 * Nc + 48 * Nf);
-		return B * (lim ? 464 * Nc + 144 * Nf : 304 * Nc + 96 * Nf);
+		if (!D->d.order2) return B * (32 * Nc + (104 + (visc ? 32 : 0)) * Nf + 48 * Nb + gather_b);
+		return B * (grad_b + face_b + gather_b);
 	case FV_KERNEL_FACE_FLUX:
-		// per cell: primitive state 32, gradients 64, centroid 16 (+ limiter 32);
-		// per face: geometry 48 (l/r 8, n and length 24, centre 16), flux 32 + spectral radii 16 out
-		return B * ((lim ? 144 : 112) * Nc + 96 * Nf);
+		return B * face_b;
+	case FV_KERNEL_GRADIENTS:
+		return B * grad_b;
 	case FV_KERNEL_JACOBIAN:
 		return B * (32 * Nc + 40 * (Nf - Nb) + 48 * Nb + 16 * w * nblk + 4 * nblk);
 	case FV_KERNEL_PRECOND_APPLY:
@@ -716,10 +731,6 @@ double bytes_model(const fv_solver *S, int which)
 		return B * (16 * w * nblk + 4 * 2 * (Nf - Nb) + 2 * 32 * Nc);
 	case FV_KERNEL_PRECOND_SETUP:
 		return B * (2 * 16 * w * nblk + 16 * w * Nc);
-	case FV_KERNEL_GRADIENTS:
-		// u in 32 + primitive state out and in 64 + centroid/area 24 + gradients out 64
-		// (+ limiter values out 32) per cell; face geometry and gradient weights 40 per face
-		return B * ((lim ? 216 : 184) * Nc + 40 * Nf);
 	}
 	return 0;
 }
