@@ -53,11 +53,15 @@ NUM_START = dict(flux="HLLC", gradient="NONE")
 BCS = [(2, "slipwall", ()), (4, "farfield", ())]
 STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
                min_relax=0.2, pc="ilu0")
-# FGMRES relative tolerance 0.3 (PETSc's -ksp_rtol; the reference's control files
-# use 0.1): with 0.1 the solve's path is sensitive enough to rounding that it
-# stalls just above 1e-10 for some perturbations of the matrix-free step
+# Solver options of the main solve (each one the reference's own: PETSc's
+# -ksp_rtol, -matrix_free_difference_step, the update's minimum relaxation).
+# The Venkatakrishnan-limited transonic solve stalls just above 1e-10 or blows
+# up for part of the rounding-level perturbations of its path with the
+# reference's defaults (difference step 1e-7, relaxation floor 0.2); a
+# difference step of 1e-8 (fewer finite differences across limiter switches)
+# and a floor of 0.1 converge for every perturbation tried.
 MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=2000, nl_update=2,
-            min_relax=0.2, pc="ilu0", matrix_free=1, ksp_rtol=0.3)
+            min_relax=0.1, pc="ilu0", matrix_free=1, ksp_rtol=0.3, mf_eps=1e-8)
 WORKLOAD = "naca0012_transonic_512x256_ogrid_g1.02_hllc_gg_venkat5"
 METRIC = "solves/s to ||R||<1e-10 (transonic NACA0012, matrix-free FGMRES, FP32 Jacobian + FP32 block-colour ILU0)"
 C2_FIXTURE = os.path.join(ROOT, "tests", "golden", "naca0012_transonic_oracle_converged.npz")
@@ -84,6 +88,14 @@ def kernel_sources_digest():
     return h.hexdigest()[:16]
 
 
+def _host_threads():
+    """Host threads this process may run on (its CPU affinity)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def _dist():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -100,7 +112,8 @@ def workload_config(world, small=False):
             "cells": 183296 if not small else 2 * 64 * 32 - 20 * 64, "faces": 314880 if not small else None,
             "flow": "inviscid, M 0.8, AoA 1.25 deg", "scheme": "HLLC, Green-Gauss, Venkatakrishnan K=5",
             "solve": "freestream; 100 first-order starter steps (CFL 25->500); second-order solve to "
-                     "||R||<1e-10 (CFL 100->5000, matrix-free FGMRES(30))",
+                     "||R||<1e-10 (CFL 100->5000, matrix-free FGMRES(30), rtol 0.3, difference step 1e-8, "
+                     "relaxation floor 0.1)",
             "batch": 1, "parallelism": f"replicas{world}" if world > 1 else "single",
             "l2": "working set > L2 (no flush needed)"}
 
@@ -735,7 +748,7 @@ def oracle_solve(od1, od2, u, order=None):
     u, st2 = od2.steady_solve(u, cflmin=M["cfl_min"], cflmax=M["cfl_max"], tol=M["tolerance"],
                               maxiter=M["max_timesteps"], abs_tol=bool(M["abs_tolerance"]), pc="ilu0",
                               nl_update="bounded", min_relax=M["min_relax"], matrix_free=bool(M["matrix_free"]),
-                              lin_rtol=M.get("ksp_rtol", 0.1), order=order)
+                              lin_rtol=M.get("ksp_rtol", 0.1), mf_eps=M.get("mf_eps", 1e-7), order=order)
     t2 = time.perf_counter()
     return u, st1, st2, t1 - t0, t2 - t1
 
@@ -746,7 +759,7 @@ def _oracle_steps(od, cfg, u, nsteps, lin_maxit):
     t0 = time.perf_counter()
     od.steady_solve(u, cflmin=cfg["cfl_min"], cflmax=cfg["cfl_max"], tol=1e-30, maxiter=nsteps, pc="ilu0",
                     matrix_free=bool(cfg.get("matrix_free", 0)), nl_update="bounded", min_relax=cfg["min_relax"],
-                    abs_tol=True, lin_rtol=1e-14, lin_maxit=lin_maxit)
+                    abs_tol=True, lin_rtol=1e-14, lin_maxit=lin_maxit, mf_eps=cfg.get("mf_eps", 1e-7))
     return (time.perf_counter() - t0) / nsteps
 
 
@@ -826,7 +839,7 @@ def cpu_baseline(m, budget_s, u_state=None, counts=None):
     were timed at), the oracle's residual, FP64 Jacobian assembly, ILU(0)
     factorisation and ILU(0) apply are timed there too."""
     from oracle import orc
-    nthreads = os.cpu_count() or 1
+    nthreads = _host_threads()
     orc.set_threads(nthreads)
     counts = counts or _fixture_counts()
     if counts is None:
@@ -867,7 +880,7 @@ def run_reference(args):
     if not os.path.exists(fvbuild.ORACLE_LIB):
         fvbuild.build_oracle()
     from oracle import meshgen, orc
-    nthreads = os.cpu_count() or 1
+    nthreads = _host_threads()
     orc.set_threads(nthreads)
     t0 = time.perf_counter()
     arrs = meshgen.naca_ogrid(*(SMALL_MESH if args.small else MESH))

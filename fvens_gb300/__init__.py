@@ -277,11 +277,13 @@ class FlowFV:
         return rc, steps, tm
 
     def autotune(self, u):
-        """Picks the residual kernels' block sizes by timing them at state u
-        (fv_disc_autotune); returns [states, gradients, faces, gather]."""
-        bs = np.zeros(4, np.int32)
-        check(lib().fv_disc_autotune(self._h, _vp(dptr(u)), _hp(bs, ctypes.c_int)))
-        return bs.tolist()
+        """Picks the block sizes of the residual kernels and of the Jacobian's
+        face kernel by timing them at state u (fv_disc_autotune); returns
+        {states, gradients, faces, gather, jacobian_faces: block size}."""
+        bs = np.zeros(5, np.int32)
+        check(lib().fv_disc_autotune(self._h, _vp(dptr(u)), None))
+        check(lib().fv_disc_block_sizes(self._h, 5, _hp(bs, ctypes.c_int)))
+        return dict(zip(("states", "gradients", "faces", "gather", "jacobian_faces"), bs.tolist()))
 
     def entropy_error(self, u):
         """FlowOutput::compute_entropy_cell per batch member."""

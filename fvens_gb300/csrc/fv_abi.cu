@@ -541,6 +541,13 @@ fv_status fv_disc_autotune(fv_disc *D, const double *u, int *h_block_sizes)
 	return cuda_status(e, "autotune");
 }
 
+fv_status fv_disc_block_sizes(const fv_disc *D, int n, int *h_block_sizes)
+{
+	if (!D || !h_block_sizes || n < 1) { set_error("null argument or n < 1"); return FV_ERR_INVALID; }
+	for (int k = 0; k < n && k < KBS_COUNT; k++) h_block_sizes[k] = D->bs[k];
+	return FV_OK;
+}
+
 fv_status fv_get_gradients(fv_disc *D, const double *u, double *grad, int primitive)
 {
 	if (!D || !u || !grad) { set_error("null argument"); return FV_ERR_INVALID; }

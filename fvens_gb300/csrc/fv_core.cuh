@@ -101,7 +101,7 @@ struct ResidualWork {
 	double2 *spec = nullptr;   // [batch][naface] spectral radii (left, right)
 };
 
-enum { KBS_PREP = 0, KBS_GRAD = 1, KBS_FACE = 2, KBS_GATHER = 3 };
+enum { KBS_PREP = 0, KBS_GRAD = 1, KBS_FACE = 2, KBS_GATHER = 3, KBS_JAC = 4, KBS_COUNT = 5 };
 
 struct fv_disc_impl {
 	fv_mesh_impl *mesh = nullptr;
@@ -113,7 +113,7 @@ struct fv_disc_impl {
 	// owned device arrays
 	std::vector<void *> owned;
 	ResidualWork w;
-	int bs[4] = {128, 128, 128, 128};  // block sizes of the residual kernels (KBS_*), fv_disc_autotune
+	int bs[KBS_COUNT] = {128, 128, 128, 128, 128};  // block sizes of the residual and Jacobian kernels (KBS_*), fv_disc_autotune
 	int *btag = nullptr;       // device: boundary marker of each boundary face
 	double *surf = nullptr;    // device: surface-integral partials [batch][4]
 	cudaStream_t stream = 0;

@@ -21,14 +21,15 @@ namespace fvg {
 namespace {
 
 constexpr int BS = 128;
+constexpr int kMaxJacBS = 256;  // bound of the face kernel's tuned block size (fv_disc_autotune)
 
 template <int JFLUX, class R>
-__global__ void __launch_bounds__(BS) k_jac_face(DiscDev D, const double *__restrict__ u, R *__restrict__ val,
-                                                 double *__restrict__ bdiag, const int2 *__restrict__ fslot)
+__global__ void __launch_bounds__(kMaxJacBS) k_jac_face(DiscDev D, const double *__restrict__ u, R *__restrict__ val,
+                                                        double *__restrict__ bdiag, const int2 *__restrict__ fslot)
 {
 	const int b = blockIdx.y;
 	if (skip_member(D, b)) return;
-	const int f = blockIdx.x * BS + threadIdx.x;
+	const int f = blockIdx.x * blockDim.x + threadIdx.x;
 	if (f >= D.naface) return;
 	jac_face_body<JFLUX, R>(D, b, f, u, val, bdiag, fslot);
 }
@@ -70,15 +71,16 @@ cudaError_t launch_all(fv_disc_impl *Dh, const double *u, BlockMatrix &A, cudaSt
 	R *val = reinterpret_cast<R *>(A.val);
 	const int2 *fslot = Dh->mesh->d.fslot;
 	const int4 *crev = Dh->mesh->d.cslot_rev;
-	const dim3 gf((unsigned)((D.naface + BS - 1) / BS), (unsigned)B);
+	const int bj = Dh->bs[KBS_JAC];
+	const dim3 gf((unsigned)((D.naface + bj - 1) / bj), (unsigned)B);
 	const dim3 gc((unsigned)((D.nelem + BS - 1) / BS), (unsigned)B);
 	k_zero_slots<R><<<gc, BS, 0, s>>>(D, val);
 	switch (D.jflux) {
-	case FLUX_LLF: k_jac_face<FLUX_LLF, R><<<gf, BS, 0, s>>>(D, u, val, A.bdiag, fslot); break;
-	case FLUX_AUSM: k_jac_face<FLUX_AUSM, R><<<gf, BS, 0, s>>>(D, u, val, A.bdiag, fslot); break;
-	case FLUX_ROE: k_jac_face<FLUX_ROE, R><<<gf, BS, 0, s>>>(D, u, val, A.bdiag, fslot); break;
-	case FLUX_HLL: k_jac_face<FLUX_HLL, R><<<gf, BS, 0, s>>>(D, u, val, A.bdiag, fslot); break;
-	case FLUX_HLLC: k_jac_face<FLUX_HLLC, R><<<gf, BS, 0, s>>>(D, u, val, A.bdiag, fslot); break;
+	case FLUX_LLF: k_jac_face<FLUX_LLF, R><<<gf, bj, 0, s>>>(D, u, val, A.bdiag, fslot); break;
+	case FLUX_AUSM: k_jac_face<FLUX_AUSM, R><<<gf, bj, 0, s>>>(D, u, val, A.bdiag, fslot); break;
+	case FLUX_ROE: k_jac_face<FLUX_ROE, R><<<gf, bj, 0, s>>>(D, u, val, A.bdiag, fslot); break;
+	case FLUX_HLL: k_jac_face<FLUX_HLL, R><<<gf, bj, 0, s>>>(D, u, val, A.bdiag, fslot); break;
+	case FLUX_HLLC: k_jac_face<FLUX_HLLC, R><<<gf, bj, 0, s>>>(D, u, val, A.bdiag, fslot); break;
 	default: return cudaErrorInvalidValue;
 	}
 	k_jac_diag<R><<<gc, BS, 0, s>>>(D, val, A.bdiag, crev);

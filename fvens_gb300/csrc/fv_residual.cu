@@ -262,11 +262,12 @@ cudaError_t gradients_launch(fv_disc_impl *Dh, const double *u, double *grad, in
 
 namespace fvg {
 
-/* Launch-geometry autotuner of the residual kernels: each kernel runs with
- * 64, 128 and 256 threads per block at state u (one warm-up, then three timed
- * launches with CUDA events) and keeps the fastest.  Every thread does the work
- * of one cell or face whatever the block size, so the choice changes timing,
- * not results. */
+/* Launch-geometry autotuner of the residual kernels and of the Jacobian's
+ * face kernel: each runs with 64, 128 and 256 threads per block at state u
+ * (one warm-up, then three timed launches with CUDA events) and keeps the
+ * fastest.  Every thread does the work of one cell or face whatever the block
+ * size, so the choice changes timing, not results.  The Jacobian is timed into
+ * a temporary FP32 matrix. */
 cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s, int *chosen)
 {
 	const DiscDev &D = Dh->d;
@@ -287,11 +288,16 @@ cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s,
 			                                                              Dh->w.lgrad, lim);
 			break;
 		case KBS_FACE: Dh->bs[KBS_FACE] = bs; face_launch(Dh, u, 1, s); break;
+		case KBS_JAC: Dh->bs[KBS_JAC] = bs; return jacobian_launch(Dh, u, J, s);
 		default: k_gather<<<grid_of(D.nelem, bs, B), bs, 0, s>>>(D, Dh->w, r, nullptr); break;
 		}
 		return cudaGetLastError();
 	};
-	for (int kind = 0; kind < 4 && !e; kind++) {
+	BlockMatrix J;
+	J.nelem = D.nelem; J.batch = B; J.prec = 4;
+	if (!e) e = cudaMalloc(&J.val, sizeof(float) * J.nval());
+	if (!e) e = cudaMalloc(&J.bdiag, sizeof(double) * 16 * (size_t)B * (D.nbface > 0 ? D.nbface : 1));
+	for (int kind = 0; kind < KBS_COUNT && !e; kind++) {
 		float best = 1e30f;
 		int pick = Dh->bs[kind];
 		for (int c = 0; c < 3 && !e; c++) {
@@ -305,9 +311,11 @@ cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s,
 			if (!e && ms < best) { best = ms; pick = cand[c]; }
 		}
 		Dh->bs[kind] = pick;
-		if (chosen) chosen[kind] = pick;
+		if (chosen && kind < 4) chosen[kind] = pick;
 	}
-	Dh->kernels_launched += 4 * 3 * 4 + 2;
+	Dh->kernels_launched += 4 * 3 * 4 + 2;  // the Jacobian's launches count themselves
+	if (J.val) cudaFree(J.val);
+	if (J.bdiag) cudaFree(J.bdiag);
 	cudaEventDestroy(a);
 	cudaEventDestroy(b);
 	if (r) cudaFree(r);

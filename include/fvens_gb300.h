@@ -178,11 +178,16 @@ void fv_disc_destroy(fv_disc *d);
 fv_status fv_disc_set_stream(fv_disc *d, void *stream);
 fv_status fv_disc_synchronize(fv_disc *d);
 /* Autotuner (no counterpart in the reference): times the residual kernels
- * (states, gradients/limiter, faces, gather) with 64, 128 and 256 threads per
- * block at device state d_u and keeps the fastest for this handle; results do
- * not depend on the choice.  h_block_sizes[4] (host, may be NULL) receives
- * the choice.  Synchronises. */
+ * (states, gradients/limiter, faces, gather) and the Jacobian's face kernel
+ * with 64, 128 and 256 threads per block at device state d_u and keeps the
+ * fastest for this handle; results do not depend on the choice.
+ * h_block_sizes[4] (host, may be NULL) receives the residual kernels' choice
+ * (fv_disc_block_sizes gives all).  Synchronises. */
 fv_status fv_disc_autotune(fv_disc *d, const double *d_u, int *h_block_sizes);
+/* The block sizes in use (no counterpart in the reference): up to n of
+ * [states, gradients, faces, gather, Jacobian faces]; fv_disc_autotune also
+ * tunes the last one. */
+fv_status fv_disc_block_sizes(const fv_disc *d, int n, int *h_block_sizes);
 /* freestream conserved states (IdealGasPhysics::compute_freestream_state), batch x 4 */
 fv_status fv_disc_freestream(const fv_disc *d, double *h_uinf);
 

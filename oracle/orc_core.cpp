@@ -1012,11 +1012,22 @@ struct Precond {
 
 // ================================= FGMRES ===================================
 
+/* dot product in a fixed order whatever the thread count: sums of blocks of
+ * 4096 entries (in parallel), then the block sums in order */
 inline double dotv(const double *a, const double *b, size_t n)
 {
+	constexpr size_t BLK = 4096;
+	const long nb = (long)((n + BLK - 1) / BLK);
+	std::vector<double> part(nb > 0 ? nb : 1, 0.0);
+#pragma omp parallel for schedule(static)
+	for (long k = 0; k < nb; k++) {
+		const size_t i1 = std::min(n, (size_t)(k + 1) * BLK);
+		double s = 0;
+		for (size_t i = (size_t)k * BLK; i < i1; i++) s += a[i] * b[i];
+		part[k] = s;
+	}
 	double s = 0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-	for (long i = 0; i < (long)n; i++) s += a[i] * b[i];
+	for (long k = 0; k < nb; k++) s += part[k];
 	return s;
 }
 

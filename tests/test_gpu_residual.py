@@ -113,8 +113,9 @@ def test_freestream_is_steady(cuda):
 
 
 def test_autotune_keeps_results(cuda):
-    """The residual kernels' block sizes picked by fv_disc_autotune change
-    timing only: the residual and local time steps are bitwise unchanged."""
+    """The block sizes picked by fv_disc_autotune (residual kernels and the
+    Jacobian's face kernel) change timing only: the residual, local time steps
+    and the FP32 Jacobian are bitwise unchanged."""
     import torch
     name, mesh, phys, num, bcs = cases.RESIDUAL_CASES[1]
     m = mesh()
@@ -122,8 +123,15 @@ def test_autotune_keeps_results(cuda):
     u = torch.tensor(cases.perturbed_state(gd.freestream()[0], m.nelem), device=cuda)
     r0, dt0 = torch.zeros_like(u), torch.zeros(m.nelem, dtype=torch.float64, device=cuda)
     gd.compute_residual(u, r0, True, dt0)
+    A0 = fv.BlockMatrix(gd, 4)
+    gd.assemble_jacobian(u, A0)
     bs = gd.autotune(u)
-    assert len(bs) == 4 and all(b in (64, 128, 256) for b in bs)
+    assert set(bs) == {"states", "gradients", "faces", "gather", "jacobian_faces"}
+    assert all(b in (64, 128, 256) for b in bs.values())
     r1, dt1 = torch.zeros_like(u), torch.zeros_like(dt0)
     gd.compute_residual(u, r1, True, dt1)
     assert torch.equal(r0, r1) and torch.equal(dt0, dt1)
+    A1 = fv.BlockMatrix(gd, 4)
+    gd.assemble_jacobian(u, A1)
+    gd.synchronize()
+    assert np.array_equal(A0.to_host()[2], A1.to_host()[2])
