@@ -276,6 +276,11 @@ cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s,
 	double *r = nullptr;
 	cudaError_t e = cudaMalloc(&r, sizeof(double) * 4 * (size_t)D.nelem * B);
 	if (!e) e = gradient_pass_launch(Dh, u, s);  // fill the scratch the later kernels read
+	// temporary FP32 matrix for timing the Jacobian
+	BlockMatrix J;
+	J.nelem = D.nelem; J.batch = B; J.prec = 4;
+	if (!e) e = cudaMalloc(&J.val, sizeof(float) * J.nval());
+	if (!e) e = cudaMalloc(&J.bdiag, sizeof(double) * 16 * (size_t)B * (D.nbface > 0 ? D.nbface : 1));
 	cudaEvent_t a, b;
 	cudaEventCreate(&a);
 	cudaEventCreate(&b);
@@ -293,10 +298,6 @@ cudaError_t residual_autotune(fv_disc_impl *Dh, const double *u, cudaStream_t s,
 		}
 		return cudaGetLastError();
 	};
-	BlockMatrix J;
-	J.nelem = D.nelem; J.batch = B; J.prec = 4;
-	if (!e) e = cudaMalloc(&J.val, sizeof(float) * J.nval());
-	if (!e) e = cudaMalloc(&J.bdiag, sizeof(double) * 16 * (size_t)B * (D.nbface > 0 ? D.nbface : 1));
 	for (int kind = 0; kind < KBS_COUNT && !e; kind++) {
 		float best = 1e30f;
 		int pick = Dh->bs[kind];
