@@ -373,6 +373,16 @@ def run_variants(fv, torch, dev, m, main, start, u0d, prec, args):
     solves (run_batched).  (3) The learned warm start (run_warm_start).
     (4) The ~4M-cell instance (run_large)."""
     out = {}
+
+    def guarded(name, fn):
+        # a variant that fails reports its error instead of ending the benchmark
+        try:
+            out[name] = fn()
+        except Exception as exc:  # noqa: BLE001
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.synchronize()
+        return out[name]
+
     u = torch.empty_like(u0d)
     P1 = fv.SteadyBackwardEulerSolver(start, precision=8, **STARTER)
     P2 = fv.SteadyBackwardEulerSolver(main, precision=8, **MAIN)
@@ -382,16 +392,22 @@ def run_variants(fv, torch, dev, m, main, start, u0d, prec, args):
                               "linear_iters": st["lin_iters"], "converged": st["status"] == 0, "res": st["res"]}
     del P1, P2
     if args.large:
-        out["large_4m"] = run_large(fv, torch, dev, float(_peaks().get("hbm_gbs", 6800.0)), args.large_solve)
+        guarded("large_4m", lambda: run_large(fv, torch, dev, float(_peaks().get("hbm_gbs", 6800.0)),
+                                              args.large_solve))
     if args.batched:
-        bl, tr_phys, tr_u = run_batched(fv, torch, dev, args.laminar_levels, args.batch, sgs=args.laminar_sgs)
-        out["batched_laminar"] = bl
-        if args.warm_test > 0 and (args.warm_train > 0 or tr_phys):
-            out["warm_start_laminar"] = run_warm_start(
+        got = {}
+
+        def batched():
+            bl, got["phys"], got["u"] = run_batched(fv, torch, dev, args.laminar_levels, args.batch,
+                                                    sgs=args.laminar_sgs)
+            return bl
+        bl = guarded("batched_laminar", batched)
+        if args.warm_test > 0 and (args.warm_train > 0 or got.get("phys")):
+            guarded("warm_start_laminar", lambda: run_warm_start(
                 fv, torch, dev, args.laminar_levels, args.warm_train, args.warm_test, args.warm_epochs, args.batch,
                 plain_single_s=bl["single_plain_fp64"]["seconds"],
-                train=None if args.warm_train > 0 else (tr_phys, tr_u))
-        del tr_u
+                train_set=None if args.warm_train > 0 else (got["phys"], got["u"])))
+        got.clear()
     return out
 
 
@@ -506,11 +522,11 @@ def run_batched(fv, torch, dev, levels=2, B=64, seed=7, sgs=False):
     return res, conv_phys, conv_states
 
 
-def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_single_s=None, train=None):
+def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_single_s=None, train_set=None):
     """Learned warm start on the laminar hybrid NACA 0012 case.
 
     Training data: the converged members of a batched solve, given as
-    train = (conditions, device states), or else n_train conditions (seed 11)
+    train_set = (conditions, device states), or else n_train conditions (seed 11)
     solved here in batches of B from freestream (starter + main).  They train
     the message-passing network (4 layers, width 64; BF16 tensor-core GEMMs,
     FP32 accumulation, Adam) on the GPU.  n_test held-out conditions (seed
@@ -530,8 +546,8 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
     phs_te = _laminar_conditions(fv, n_test, 12)
     ev = lambda: torch.cuda.Event(enable_timing=True)
     keep_phys, keep_u, gen_s = [], [], 0.0
-    if train is not None:
-        keep_phys, keep_u = list(train[0]), list(train[1])
+    if train_set is not None:
+        keep_phys, keep_u = list(train_set[0]), list(train_set[1])
         n_train = 0
     for s in range(0, n_train, B):
         plist = phs_tr[s:s + B]
@@ -557,7 +573,7 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
     torch.cuda.synchronize()
     train_s = a.elapsed_time(b) / 1e3
     del targets, keep_u
-    out = {"mesh_cells": m.nelem, "train_conditions": n_train if train is None else "the batched variant's members",
+    out = {"mesh_cells": m.nelem, "train_conditions": n_train if train_set is None else "the batched variant's members",
            "train_converged": len(keep_phys),
            "test_conditions": n_test, "epochs": epochs, "train_batch": 16, "params": net.nparams,
            "data_generation_s": gen_s, "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
