@@ -58,7 +58,7 @@ class fv_bc_cfg(ctypes.Structure):
 
 
 _lib = None
-ABI_VERSION = 2  # FVENS_GB300_ABI_VERSION of include/fvens_gb300.h
+ABI_VERSION = 3  # FVENS_GB300_ABI_VERSION of include/fvens_gb300.h
 
 
 def lib():
@@ -429,7 +429,8 @@ class fv_solver_cfg(ctypes.Structure):
                 ("ksp_restart", ctypes.c_int), ("ksp_maxit", ctypes.c_int), ("ksp_rtol", ctypes.c_double),
                 ("matrix_free", ctypes.c_int), ("mf_eps", ctypes.c_double), ("nl_update", ctypes.c_int),
                 ("min_relax", ctypes.c_double), ("precision", ctypes.c_int), ("check_every", ctypes.c_int),
-                ("use_graph", ctypes.c_int), ("pc_ordering", ctypes.c_int), ("pc_part_size", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("pc_ordering", ctypes.c_int), ("pc_part_size", ctypes.c_int),
+                ("stall_steps", ctypes.c_int), ("stall_factor", ctypes.c_double)]
 
 
 class fv_solve_stats(ctypes.Structure):

@@ -36,7 +36,9 @@ constexpr int RBS = 256;
 /* per-member solver scalars (device) */
 struct StepState {
 	double *res, *resold, *res0, *cfl, *pm;  // [batch]
+	double *res_ref;                          // [batch] stagnation reference residual
 	int *step, *status, *active;              // [batch]
+	int *ref_step;                            // [batch] step at which res_ref was set
 	int *pc_err;                              // [batch] singular preconditioner block
 	double *hist;                             // [maxiter][batch][3]: res, cfl, linear iterations
 	int *linits;                              // [batch] cumulative linear iterations
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(RBS) k_update(int N, int nblk, double *__restr
 
 /* norm, NaN check, step count, convergence (aodesolver.cpp:516-537, 608-626) */
 __global__ void k_norm(int B, int nblk, const double *__restrict__ part, StepState S, const int *__restrict__ kiters,
-                       double tol, int abs_tol, int maxiter)
+                       double tol, int abs_tol, int maxiter, int stall_steps, double stall_factor)
 {
 	const int b = blockIdx.x;
 	if (b >= B || !S.active[b]) return;
@@ -171,10 +173,21 @@ __global__ void k_norm(int B, int nblk, const double *__restrict__ part, StepSta
 	if (step == 0) S.res0[b] = res;
 	S.step[b] = step + 1;
 	const bool conv = abs_tol ? (res <= tol) : (res / S.res0[b] <= tol);
+	// stagnation: the residual must fall below stall_factor times the
+	// reference value within stall_steps steps, or the member stops
+	bool stalled = false;
+	if (stall_steps > 0) {
+		if (step == 0 || res < stall_factor * S.res_ref[b]) {
+			S.res_ref[b] = res;
+			S.ref_step[b] = step;
+		} else {
+			stalled = step - S.ref_step[b] >= stall_steps;
+		}
+	}
 	if (conv) {
 		S.status[b] = ST_CONVERGED;
 		S.active[b] = 0;
-	} else if (step + 1 >= maxiter) {
+	} else if (step + 1 >= maxiter || stalled) {
 		S.status[b] = ST_TOLERANCE;
 		S.active[b] = 0;
 	}
@@ -346,7 +359,8 @@ cudaError_t solver_step(fv_solver *S, double *u, cudaStream_t s, int *nk, int *n
 	if ((e = fgmres_solve(S->K, op, S->P, S->r, S->du, c.ksp_maxit, c.ksp_rtol, S->S.active, s, nk, nk_iter))) return e;
 	k_update<<<dim3(S->nblk, B), RBS, 0, s>>>(N, S->nblk, u, S->du, S->r, D->d.area, D->d.phys, c.nl_update,
 	                                           c.min_relax, S->part, S->S);
-	k_norm<<<B, 32, 0, s>>>(B, S->nblk, S->part, S->S, S->K.iters, c.tolerance, c.abs_tolerance, c.max_timesteps);
+	k_norm<<<B, 32, 0, s>>>(B, S->nblk, S->part, S->S, S->K.iters, c.tolerance, c.abs_tolerance, c.max_timesteps,
+	                        c.stall_steps, c.stall_factor);
 	*nk += 2;
 	return cudaGetLastError();
 }
@@ -459,6 +473,7 @@ void fv_solver_cfg_default(fv_solver_cfg *c)
 	c->pc_type = FV_PC_ILU0; c->ksp_restart = 30; c->ksp_maxit = 30; c->ksp_rtol = 0.1;
 	c->matrix_free = 0; c->mf_eps = 1e-7; c->nl_update = 0; c->min_relax = 0.2; c->precision = 4;
 	c->check_every = 4; c->use_graph = 1; c->pc_ordering = 1; c->pc_part_size = 128;
+	c->stall_steps = 0; c->stall_factor = 0.5;
 }
 
 fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out)
@@ -471,6 +486,10 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	if (D->d.jflux == FV_FLUX_VANLEER || D->d.jflux == FV_FLUX_AUSMPLUS) {
 		set_error("the Jacobian flux has no Jacobian in the reference (VanLeer / AUSM+)");
 		return FV_ERR_UNSUPPORTED;
+	}
+	if (cfg->stall_steps < 0 || (cfg->stall_steps > 0 && !(cfg->stall_factor > 0.0 && cfg->stall_factor <= 1.0))) {
+		set_error("stall_steps >= 0 and, when set, 0 < stall_factor <= 1");
+		return FV_ERR_INVALID;
 	}
 	if (cfg->pc_part_size > kMaxPartSize) {
 		set_error("pc_part_size at most " + std::to_string(kMaxPartSize));
@@ -505,6 +524,8 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	if (!e) e = salloc(S, &S->S.res, B);
 	if (!e) e = salloc(S, &S->S.resold, B);
 	if (!e) e = salloc(S, &S->S.res0, B);
+	if (!e) e = salloc(S, &S->S.res_ref, B);
+	if (!e) e = salloc(S, &S->S.ref_step, B);
 	if (!e) e = salloc(S, &S->S.cfl, B);
 	if (!e) e = salloc(S, &S->S.pm, B);
 	if (!e) e = salloc(S, &S->S.step, B);

@@ -38,8 +38,9 @@ extern "C" {
 /* ABI version of this header.  A caller compiled against it checks
  * fv_abi_version() == FVENS_GB300_ABI_VERSION after loading the library.
  *   1  first release
- *   2  fv_mesh_line_ordering gained its `rcm` argument (before `order`) */
-#define FVENS_GB300_ABI_VERSION 2
+ *   2  fv_mesh_line_ordering gained its `rcm` argument (before `order`)
+ *   3  fv_solver_cfg gained stall_steps and stall_factor (at its end) */
+#define FVENS_GB300_ABI_VERSION 3
 
 typedef int fv_status;
 #define FV_OK 0
@@ -285,6 +286,11 @@ typedef struct {
 	int use_graph;             /* replay each step as a captured CUDA graph */
 	int pc_ordering;           /* 1 block colours (default), 0 point colours */
 	int pc_part_size;          /* cells per part of the block-colour order (default 128, at most 256) */
+	int stall_steps;           /* stagnation stop (not in the reference): 0 off (default); else a
+	                              member whose residual has not fallen below stall_factor times
+	                              its last reference value within stall_steps steps ends with
+	                              FV_ERR_TOLERANCE before max_timesteps */
+	double stall_factor;       /* default 0.5 */
 } fv_solver_cfg;
 typedef struct {
 	int steps, lin_iters, status; /* status: FV_OK, FV_ERR_NUMERICAL, FV_ERR_TOLERANCE */

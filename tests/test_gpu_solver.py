@@ -206,3 +206,27 @@ def test_matrix_free_first_order_matches_matrix_based(cuda):
     assert sa[0]["status"] == 0 and sb[0]["status"] == 0
     assert abs(sa[0]["steps"] - sb[0]["steps"]) <= 1, (sa[0]["steps"], sb[0]["steps"])
     assert (ua - ub).abs().max().item() <= 1e-6 * ua.abs().max().item()
+
+
+def test_stagnation_stop(cuda):
+    """stall_steps (not in the reference): a member whose residual stops
+    falling ends early with FV_ERR_TOLERANCE; a converging solve is unchanged
+    by it.  The unreachable tolerance (1e-30) makes every step after the
+    rounding floor a stall."""
+    import torch
+    m, gd, od = _setup()
+    u0 = torch.tensor(np.tile(od.freestream(), (m.nelem, 1)), device=cuda)
+    kw = dict(cfl_min=10, cfl_max=1000, pc="ilu0", precision=4)
+    ud = u0.clone()
+    rc, st = fv.SteadyBackwardEulerSolver(gd, tolerance=1e-30, max_timesteps=2000, stall_steps=20,
+                                          **kw).solve(ud, raise_on_error=False)
+    assert rc == fv.FV_ERR_TOLERANCE and st[0]["status"] == fv.FV_ERR_TOLERANCE
+    assert 20 < st[0]["steps"] < 2000 and st[0]["res"] < 1e-12
+    # converging: identical path and state with and without the stop
+    ua, ub = u0.clone(), u0.clone()
+    _, sa = fv.SteadyBackwardEulerSolver(gd, tolerance=1e-10, max_timesteps=200, **kw).solve(ua)
+    _, sb = fv.SteadyBackwardEulerSolver(gd, tolerance=1e-10, max_timesteps=200, stall_steps=20,
+                                         **kw).solve(ub)
+    assert sa[0]["steps"] == sb[0]["steps"] and torch.equal(ua, ub)
+    with pytest.raises(fv.FvensError):
+        fv.SteadyBackwardEulerSolver(gd, stall_steps=10, stall_factor=1.5, **kw)
