@@ -447,9 +447,12 @@ def _laminar_conditions(fv, n, seed):
 # in 300 steps (the solver's stagnation stop; members that converge halve it
 # every few steps): about half of the 64 conditions never converge on this
 # mesh (unsteady separated flows) and otherwise run to the step limit
+# pc_ordering 2: the preconditioner's parts coloured with one colour fewer
+# (one launch fewer per sweep) than the greedy colouring of the headline solve
 LAMINAR_MAIN = dict(cfl_min=200, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=1500, nl_update=2,
-                    stall_steps=300, stall_factor=0.5)
-LAMINAR_START = dict(cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0, max_timesteps=50, nl_update=2)
+                    stall_steps=300, stall_factor=0.5, pc_ordering=2)
+LAMINAR_START = dict(cfl_min=200, cfl_max=1000, tolerance=1e-1, abs_tolerance=0, max_timesteps=50, nl_update=2,
+                     pc_ordering=2)
 
 
 def _laminar_solvers(fv, m, plist, prec, starter=True, pc="ilu0"):

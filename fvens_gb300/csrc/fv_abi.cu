@@ -688,8 +688,17 @@ fv_status fv_pointwise_bc(fv_disc *D, int bc_type, const double *vals, int n, co
 
 extern "C" fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *nparts, int *ncolors)
 {
-	if (!m || !order || part_size < 1) { set_error("invalid argument"); return FV_ERR_INVALID; }
-	const BlockOrder bo = block_colour_order(m->h, part_size);
+	return fv_mesh_block_order_ex(m, part_size, 0, order, nparts, ncolors);
+}
+
+extern "C" fv_status fv_mesh_block_order_ex(const fv_mesh *m, int part_size, int colouring, int *order, int *nparts,
+                                            int *ncolors)
+{
+	if (!m || !order || part_size < 1 || colouring < 0 || colouring > 1) {
+		set_error("invalid argument");
+		return FV_ERR_INVALID;
+	}
+	const BlockOrder bo = block_colour_order(m->h, part_size, colouring);
 	std::memcpy(order, bo.pos_cell.data(), sizeof(int) * bo.pos_cell.size());
 	if (nparts) *nparts = bo.nparts;
 	if (ncolors) *ncolors = bo.ncolors;

@@ -986,7 +986,8 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec, int ordering, int part_size)
 {
 	P.type = type;
-	P.ordering = ordering;
+	const int colouring = ordering == 2 ? 1 : 0;
+	P.ordering = ordering ? 1 : 0;
 	P.part_size = part_size;
 	P.prec = prec;
 	P.batch = batch;
@@ -996,7 +997,7 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 	std::vector<int> pos_cell, cell_pos(N);
 	std::vector<int> part_ptr, lev_ptr, lev_pos;
 	if (P.ordering == 1) {
-		const BlockOrder bo = block_colour_order(h, P.part_size);
+		const BlockOrder bo = block_colour_order(h, P.part_size, colouring);
 		P.ncolors = bo.ncolors;
 		P.cpart = bo.cpart_ptr;
 		pos_cell = bo.pos_cell;

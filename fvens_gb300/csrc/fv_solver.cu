@@ -378,7 +378,8 @@ fv_status fv_precond_create(fv_disc *D, fv_matrix *M, int type, int ordering, in
 	fv_precond *p = new fv_precond();
 	p->D = D;
 	p->M = M;
-	cudaError_t e = precond_alloc(p->P, D->mesh, D->batch, type, M->A.prec, ordering ? 1 : 0, part_size > 0 ? part_size : 128);
+	cudaError_t e = precond_alloc(p->P, D->mesh, D->batch, type, M->A.prec, ordering < 0 || ordering > 2 ? 1 : ordering,
+	                              part_size > 0 ? part_size : 128);
 	p->P.A = &M->A;
 	if (!e) e = cudaMalloc(&p->err, sizeof(int) * D->batch);
 	if (!e) e = cudaMemset(p->err, 0, sizeof(int) * D->batch);
@@ -512,7 +513,7 @@ fv_status fv_solver_create(fv_disc *D, const fv_solver_cfg *cfg, fv_solver **out
 	cudaError_t e = cudaSuccess;
 	if (!e) e = salloc(S, (char **)&S->A.val, S->A.nval() * cfg->precision);
 	if (!e) e = salloc(S, &S->A.bdiag, 16 * (size_t)B * std::max(D->d.nbface, 1));
-	if (!e) e = precond_alloc(S->P, D->mesh, B, cfg->pc_type, cfg->precision, cfg->pc_ordering ? 1 : 0,
+	if (!e) e = precond_alloc(S->P, D->mesh, B, cfg->pc_type, cfg->precision, cfg->pc_ordering,
 	                          cfg->pc_part_size > 0 ? cfg->pc_part_size : 128);
 	S->P.A = &S->A;
 	if (!e) e = krylov_alloc(S->K, 4 * N, B, cfg->ksp_restart);

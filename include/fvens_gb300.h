@@ -132,6 +132,12 @@ fv_status fv_mesh_geometry(const fv_mesh *m, int *face_lr, double *fnorm, double
 /* block-colour elimination order of the SGS / ILU(0) preconditioners
  * (compact parts of ~part_size cells, parts coloured): order[position] = cell */
 fv_status fv_mesh_block_order(const fv_mesh *m, int part_size, int *order, int *nparts, int *ncolors);
+/* fv_mesh_block_order with the parts coloured greedily (colouring 0, as
+ * fv_mesh_block_order) or by DSatur with Kempe-chain interchanges (1: usually
+ * one colour, so one launch per sweep, fewer); the orders of fv_solver_cfg
+ * pc_ordering 1 and 2 */
+fv_status fv_mesh_block_order_ex(const fv_mesh *m, int part_size, int colouring, int *order, int *nparts,
+                                 int *ncolors);
 /* Lines of strongly coupled cells (findLines, meshordering.cpp:131-262; the
  * reference's -mesh_reorder line -mesh_anisotropy_threshold): from the cell
  * of each boundary face, follow the neighbour of largest (1/distance) weight,
@@ -284,7 +290,8 @@ typedef struct {
 	int precision;             /* stored Jacobian and preconditioner: 4 FP32, 8 FP64 */
 	int check_every;           /* steps between host polls of the convergence flags */
 	int use_graph;             /* replay each step as a captured CUDA graph */
-	int pc_ordering;           /* 1 block colours (default), 0 point colours */
+	int pc_ordering;           /* 1 block colours (default), 2 block colours with fewer colours
+	                              (fv_mesh_block_order_ex colouring 1), 0 point colours */
 	int pc_part_size;          /* cells per part of the block-colour order (default 128, at most 256) */
 	int stall_steps;           /* stagnation stop (not in the reference): 0 off (default); else a
 	                              member whose residual has not fallen below stall_factor times

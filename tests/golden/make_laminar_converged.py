@@ -4,8 +4,11 @@ converged solves of the first members of bench.py's batched laminar workload
 Re ~ U[2000, 10000]) on the reference's hybrid NACA 0012 mesh refined
 `levels` times (fvens_gb300.meshes.refine; cells in the refinement's order):
 first-order starter, then the second-order solve (Roe, least squares,
-adiabatic wall) to an absolute 1e-10, natural-order ILU(0), the bench's CFL
-settings.
+adiabatic wall) to an absolute 1e-10, the bench's CFL settings, ILU(0) in the
+GPU's elimination order (block colours with the boundary-layer lines kept
+whole, from the product library here, in the refinement's cell numbering;
+with the natural order the oracle's solve of member 0 stalls at 1.4e-6 after
+1,500 steps).
 
     python tests/golden/make_laminar_converged.py [levels] [members] [threads]
 
@@ -29,13 +32,30 @@ from fvens_gb300 import meshes  # noqa: E402
 from oracle import orc  # noqa: E402
 
 
+def block_order(a):
+    """The GPU's elimination order for the bench's laminar mesh (RCM, lines at
+    threshold 10, parts of 128 coloured as pc_ordering 2), as cells of the
+    array numbering of a."""
+    import ctypes
+
+    import fvens_gb300 as fv
+    m = fv.UMesh.from_arrays(a["coords"], a["nnode"], a["inpoel"], a["bface"], a["btag"], reorder=1)
+    m.find_lines(10.0)
+    order = np.zeros(m.nelem, np.int32)
+    npart, ncol = ctypes.c_int(), ctypes.c_int()
+    fv.check(fv.lib().fv_mesh_block_order_ex(m._h, 128, 1, fv._hp(order, ctypes.c_int), ctypes.byref(npart),
+                                             ctypes.byref(ncol)))
+    return m.export()["perm"][order].astype(np.int32)
+
+
 def main(levels, members, threads):
     from fvens_gb300 import build
-    build.build_oracle()
+    build.build_all()
     orc.set_threads(threads)
     z = np.load(os.path.join(HERE, "naca0012_lam_hybrid_1_mesh.npz"))
     a = meshes.refine(dict(coords=z["coords"], nnode=z["nnode"], inpoel=z["inpoel"], bface=z["bface"],
                            btag=z["btag"]), levels)
+    order = block_order(a)
     om = orc.Mesh(a["coords"], a["nnode"], a["inpoel"], a["bface"], a["btag"])
     wall_nodes = np.unique(a["bface"][a["btag"] == 2])
     near_wall = np.where(np.isin(a["inpoel"], wall_nodes).any(axis=1))[0]
@@ -55,9 +75,10 @@ def main(levels, members, threads):
         t0 = time.perf_counter()
         u, s1 = d1.steady_solve(np.tile(d2.freestream(), (om.nelem, 1)), cflmin=S["cfl_min"], cflmax=S["cfl_max"],
                                 tol=S["tolerance"], maxiter=S["max_timesteps"], abs_tol=False, pc="ilu0",
-                                nl_update="bounded")
+                                nl_update="bounded", order=order)
         u, s2 = d2.steady_solve(u, cflmin=T["cfl_min"], cflmax=T["cfl_max"], tol=T["tolerance"],
-                                maxiter=T["max_timesteps"], abs_tol=True, pc="ilu0", nl_update="bounded")
+                                maxiter=T["max_timesteps"], abs_tol=True, pc="ilu0", nl_update="bounded",
+                                order=order)
         f = d2.surface_data(u, 2)
         print("member", k, "starter", s1["steps"], "main", s2["steps"], s2["lin_iters"], "status", s2["status"],
               f"res {s2['res']:.2e}", "Cl CDp CDsf", f.tolist(), f"{time.perf_counter() - t0:.0f} s", flush=True)
@@ -67,7 +88,7 @@ def main(levels, members, threads):
         funs.append(f)
         counts.append([s1["steps"], s1["lin_iters"], s2["steps"], s2["lin_iters"]])
     np.savez_compressed(os.path.join(HERE, f"naca0012_laminar_l{levels}_oracle_converged.npz"),
-                        members=np.array(members, np.int32), cells=cells, states=np.array(states),
+                        members=np.array(members, np.int32), order=order, cells=cells, states=np.array(states),
                         functionals=np.array(funs), solve_counts=np.array(counts, np.int64))
 
 

@@ -31,7 +31,7 @@ def _system(cuda, prec, mesh=None):
 
 @pytest.mark.parametrize("prec,tol", [(8, 1e-11), (4, 3e-5)])
 @pytest.mark.parametrize("kind", ["jacobi", "sgs", "ilu0"])
-@pytest.mark.parametrize("ordering", [1, 0])
+@pytest.mark.parametrize("ordering", [1, 2, 0])
 def test_precond_apply(cuda, prec, tol, kind, ordering):
     import torch
     m, gd, A, rp, col, val = _system(cuda, prec)
@@ -46,9 +46,10 @@ def test_precond_apply(cuda, prec, tol, kind, ordering):
     assert err <= tol, f"{kind} prec {prec} ordering {ordering}: {err:.3e}"
 
 
-def test_block_order_is_valid(cuda):
+@pytest.mark.parametrize("ordering", [1, 2])
+def test_block_order_is_valid(cuda, ordering):
     m, gd, A, rp, col, val = _system(cuda, 8, mesh=cases.channel(96, 32))
-    P = fv.Preconditioner(gd, A, "ilu0", ordering=1, part_size=128)
+    P = fv.Preconditioner(gd, A, "ilu0", ordering=ordering, part_size=128)
     order = P.order()
     assert np.array_equal(np.sort(order), np.arange(m.nelem))
 

@@ -94,6 +94,24 @@ def test_colourings_are_proper():
     assert npart.value >= m.nelem // 64 and ncol.value <= 8
 
 
+def test_fewer_colour_part_colouring():
+    """fv_mesh_block_order_ex colouring 1 (DSatur + Kempe interchanges): as
+    many parts as the greedy colouring and 4 colours on the transonic NACA 0012
+    O-grid where greedy needs 5 (the preconditioners in that order match the
+    oracle's: test_gpu_linalg.py)."""
+    import ctypes
+    m = fv.UMesh.generate(fv.MESH_NACA_OGRID, [512, 256, 30.0, 0, 0, 1.02, 154, 3], reorder=1)
+    res = {}
+    for col in (0, 1):
+        order = np.zeros(m.nelem, np.int32)
+        npart, ncol = ctypes.c_int(), ctypes.c_int()
+        fv.check(fv.lib().fv_mesh_block_order_ex(m._h, 128, col, fv._hp(order, ctypes.c_int), ctypes.byref(npart),
+                                                 ctypes.byref(ncol)))
+        assert np.array_equal(np.sort(order), np.arange(m.nelem))
+        res[col] = (npart.value, ncol.value, order)
+    assert res[0][0] == res[1][0] and (res[0][1], res[1][1]) == (5, 4)
+
+
 @pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference test meshes not present")
 @pytest.mark.parametrize("name", ["testperiodic.msh", "2dcylinderhybrid.msh", "testhybrid.msh"])
 def test_gmsh_reader_on_reference_meshes(name):
