@@ -15,7 +15,8 @@ with the natural order the oracle's solve of member 0 stalls at 1.4e-6 after
 Stored per member: the converged state at 4,096 seeded cells and at every
 cell touching the wall (`cells`, `states`), Cl / CDp / CDsf (`functionals`)
 and the step and Krylov counts.  bench.py compares the GPU's converged batch
-members with it.  Takes tens of minutes per member on a few cores.
+members with it.  Member 0 took 2,443 s on 7 x86 threads (50 + 681 steps,
+1,128 + 18,664 Krylov iterations).
 """
 import os
 import sys
@@ -88,7 +89,7 @@ def main(levels, members, threads):
         funs.append(f)
         counts.append([s1["steps"], s1["lin_iters"], s2["steps"], s2["lin_iters"]])
     np.savez_compressed(os.path.join(HERE, f"naca0012_laminar_l{levels}_oracle_converged.npz"),
-                        members=np.array(members, np.int32), order=order, cells=cells, states=np.array(states),
+                        members=np.array(members, np.int32), cells=cells, states=np.array(states),
                         functionals=np.array(funs), solve_counts=np.array(counts, np.int64))
 
 
