@@ -554,7 +554,7 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
     FP64 solve."""
     import collections
 
-    from fvens_gb300.mpnn import MPNN, fallback_solve, output_scale, train
+    from fvens_gb300.mpnn import MPNN, diverged, fallback_solve, output_scale, train
     m, _ = _laminar_mesh(fv, levels)
     phs_tr = _laminar_conditions(fv, n_train, 11)
     phs_te = _laminar_conditions(fv, n_test, 12)
@@ -592,7 +592,7 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
            "test_conditions": n_test, "epochs": epochs, "train_batch": 16, "params": net.nparams,
            "data_generation_s": gen_s, "training_s": train_s, "loss_first_last": [losses[0], losses[-1]]}
     agg = {k: dict(seconds=0.0, steps=[], res0=[], status=collections.Counter()) for k in ("freestream", "warm")}
-    fb = dict(seconds=0.0, members=0, converged=0)
+    fb = dict(seconds=0.0, members=0, converged=0, stalled_kept=0, free_converged_of_kept=0)
     err_ratio, du, dcl, dcd, pred_s = [], [], [], [], 0.0
     for s in range(0, n_test, B):
         plist = phs_te[s:s + B]
@@ -613,7 +613,9 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
         u0_warm = u_warm.clone()
         t, st_warm = _timed_solve(torch, solvers_w, u_warm, all_members=True)
         agg["warm"]["seconds"] += t + a.elapsed_time(b) / 1e3
-        # the network's result judged: members that did not converge restart from freestream
+        # the network's result judged: members whose solve from the prediction diverged (or
+        # ended no lower than it started) restart from freestream; a stall or the step limit
+        # is kept (mpnn.diverged)
         st_fb = [dict(x) for x in st_warm]
         starter_fb = fv.SteadyBackwardEulerSolver(
             fv.FlowFV(m, plist, fv.numerics_cfg(flux="ROE", gradient="NONE"), LAMINAR_BCS), pc="ilu0", precision=4,
@@ -621,7 +623,10 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
         u_fb = u_warm.clone()
         a2, b2 = ev(), ev()
         a2.record()
-        fell = fallback_solve(main_w, starter_fb, solvers_w[-1], u_fb, st_fb)
+        fell = fallback_solve(main_w, starter_fb, solvers_w[-1], u_fb, st_fb, judge=diverged)
+        fb["stalled_kept"] += sum(1 for x in st_warm if x["status"] != 0) - len(fell)
+        fb["free_converged_of_kept"] += sum(1 for k, x in enumerate(st_warm)
+                                            if x["status"] != 0 and k not in fell and st_free[k]["status"] == 0)
         b2.record()
         torch.cuda.synchronize()
         fb["seconds"] += a2.elapsed_time(b2) / 1e3
@@ -661,7 +666,11 @@ def run_warm_start(fv, torch, dev, levels, n_train, n_test, epochs, B=64, plain_
     out["warm"]["prediction_s"] = pred_s
     fb_s = out["warm"]["seconds"] + fb["seconds"]
     out["warm_with_fallback"] = {"seconds": fb_s, "converged": fb["converged"], "fallback_members": fb["members"],
-                                 "fallback_s": fb["seconds"], "converged_solves_s": fb["converged"] / fb_s}
+                                 "fallback_s": fb["seconds"], "converged_solves_s": fb["converged"] / fb_s,
+                                 "judge": "fall back when the solve from the prediction diverged or ended no lower "
+                                          "than it started; a stall or the step limit is kept",
+                                 "stalled_kept": fb["stalled_kept"],
+                                 "stalled_kept_converged_from_freestream": fb["free_converged_of_kept"]}
     out["initial_error_ratio_mean"] = float(np.mean(err_ratio)) if err_ratio else None
     out["initial_error_ratio_max"] = float(np.max(err_ratio)) if err_ratio else None
     q = lambda v, f: float(np.quantile(v, f)) if v else None
@@ -1017,24 +1026,26 @@ def _kernel_mpnn(fv, torch, dev, B, steps):
     tgt = torch.empty((B * m.nelem, 4), dtype=torch.float64, device=dev)
     net.predict(phs, tgt)
     tgt *= 1.01
-    for _ in range(3):
-        net.train_step(phs, tgt, 1e-4)
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(steps):
-        net.train_step(phs, tgt, 1e-4)
-    b.record()
-    torch.cuda.synchronize()
-    t_train = a.elapsed_time(b) / steps
     u = torch.empty_like(tgt)
-    a.record()
-    for _ in range(steps):
-        net.predict(phs, u)
-    b.record()
-    torch.cuda.synchronize()
-    print(f"mpnn: train step {t_train:.3f} ms, predict {a.elapsed_time(b) / steps:.3f} ms, "
-          f"{B} conditions x {m.nelem} cells")
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for path in ("mma_sync", "tcgen05"):  # the default path first (a launch list of the first launches covers it)
+        net.set_gemm_path(path)
+        for _ in range(3):
+            net.train_step(phs, tgt, 1e-4)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(steps):
+            net.train_step(phs, tgt, 1e-4)
+        b.record()
+        torch.cuda.synchronize()
+        t_train = a.elapsed_time(b) / steps
+        a.record()
+        for _ in range(steps):
+            net.predict(phs, u)
+        b.record()
+        torch.cuda.synchronize()
+        print(f"mpnn ({path} forward GEMMs): train step {t_train:.3f} ms, predict {a.elapsed_time(b) / steps:.3f} ms, "
+              f"{B} conditions x {m.nelem} cells")
 
 
 def main():

@@ -28,18 +28,23 @@
  * mma.sync (m16n8k16) with FP32 accumulation: GEMM operands (weights and
  * activations, S) are rounded to BF16 when they are staged in shared memory;
  * activations, biases, gradients and the Adam state stay FP32.  The GEMMs are
- * small (K <= 128, N <= 128), far from the solver's hot path.
+ * small (K <= 128, N <= 128), far from the solver's hot path.  Where a GEMM's
+ * row operand is a contiguous block of FP32 rows, bulk copies (the TMA
+ * engine) stage the CTA's next tiles while it multiplies the current one.
  * Reductions over rows (weight gradients, aggregation) run in fixed order.
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <random>
 #include <vector>
 
 #include "fv_abi_internal.hpp"
+#include "fv_bulk.cuh"
+#include "fv_tc05.cuh"
 
 namespace fvg {
 namespace {
@@ -95,28 +100,6 @@ __device__ __forceinline__ void tile_mma(const __nv_bfloat16 *sA, const __nv_bfl
 			mma_bf16(c[nt], af, bf);
 		}
 	}
-}
-
-/* stores the accumulators of a tile: rows r (< nrows), columns n < ncols */
-template <int N>
-__device__ __forceinline__ void tile_store(const float (*c)[4], int row0, int nrows, const float *bias, float *out,
-                                           int ldo, int ncols, float *pre, int relu)
-{
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int g = lane >> 2, t = lane & 3;
-	for (int nt = 0; nt < N / 8; nt++)
-		for (int h = 0; h < 2; h++) {
-			const int r = row0 + warp * 16 + g + 8 * h;
-			if (r >= nrows) continue;
-			for (int j = 0; j < 2; j++) {
-				const int n = nt * 8 + 2 * t + j;
-				if (n >= ncols) continue;
-				float v = c[nt][2 * h + j] + (bias ? bias[n] : 0.f);
-				if (pre) pre[(size_t)r * ldo + n] = v;
-				if (relu) v = fmaxf(v, 0.f);
-				out[(size_t)r * ldo + n] = v;
-			}
-		}
 }
 
 /* stage B = W [N][K] (fp32, row stride ldw) as bf16 into shared memory */
@@ -175,15 +158,6 @@ struct LEnc {  // [xs (4), M, AoA, Re (3), 0...]: K = 16
 		return make_float4(0.f, 0.f, 0.f, 0.f);
 	}
 };
-struct LUpd {  // [h (64), a (64)]: K = 128
-	const float *h, *agg;
-	__device__ void prep(int, RowInfo &) const {}
-	__device__ float4 quad(int r, const RowInfo &, int q) const
-	{
-		return q < W / 4 ? reinterpret_cast<const float4 *>(h + (size_t)r * W)[q]
-		                 : reinterpret_cast<const float4 *>(agg + (size_t)r * W)[q - W / 4];
-	}
-};
 struct LRows {  // plain rows x[r][0..nz) (row stride ld, both multiples of 4), zero beyond
 	const float *x;
 	int ld, nz;
@@ -218,11 +192,24 @@ __device__ __forceinline__ void stage_rows(const L &ld, int row0, int rows, RowI
 }
 
 // ----------------------------------- epilogues -----------------------------------
+/* An epilogue gets columns n, n + 1 (n even) of output row r.  old(r, n) reads
+ * what it adds to (or zeros): the kernels read it for all of a tile's
+ * positions before the tile's MMAs, so those loads overlap the multiply
+ * instead of waiting one by one between the stores. */
 struct EStore {  // out = act(Z + bias) (pre = Z + bias when given), columns < ncols (even)
 	const float *bias;
 	float *out, *pre;
 	int ldo, ncols, relu;
-	__device__ void operator()(int r, int n, float z0, float z1) const  // columns n, n + 1 (n even)
+	__device__ float2 old(int, int) const { return make_float2(0.f, 0.f); }
+	__device__ float4 old4(int, int) const { return make_float4(0.f, 0.f, 0.f, 0.f); }
+	__device__ void put4(int r, int n, float4 z, float4) const  // columns n..n+3 (n % 4 == 0, n + 4 <= ncols)
+	{
+		const float4 v = bias ? make_float4(z.x + bias[n], z.y + bias[n + 1], z.z + bias[n + 2], z.w + bias[n + 3]) : z;
+		if (pre) *reinterpret_cast<float4 *>(pre + (size_t)r * ldo + n) = v;
+		*reinterpret_cast<float4 *>(out + (size_t)r * ldo + n) =
+		    relu ? make_float4(fmaxf(v.x, 0.f), fmaxf(v.y, 0.f), fmaxf(v.z, 0.f), fmaxf(v.w, 0.f)) : v;
+	}
+	__device__ void operator()(int r, int n, float z0, float z1, float2) const
 	{
 		if (n >= ncols) return;
 		const float2 v = make_float2(z0 + (bias ? bias[n] : 0.f), z1 + (bias ? bias[n + 1] : 0.f));
@@ -234,10 +221,18 @@ struct EStore {  // out = act(Z + bias) (pre = Z + bias when given), columns < n
 struct EUpdate {  // hn = h + relu(Z + bu), pre = Z + bu
 	const float *bias, *h;
 	float *hn, *pre;
-	__device__ void operator()(int r, int n, float z0, float z1) const
+	__device__ float2 old(int r, int n) const { return *reinterpret_cast<const float2 *>(h + (size_t)r * W + n); }
+	__device__ float4 old4(int r, int n) const { return *reinterpret_cast<const float4 *>(h + (size_t)r * W + n); }
+	__device__ void put4(int r, int n, float4 z, float4 hh) const
+	{
+		const float4 v = make_float4(z.x + bias[n], z.y + bias[n + 1], z.z + bias[n + 2], z.w + bias[n + 3]);
+		*reinterpret_cast<float4 *>(pre + (size_t)r * W + n) = v;
+		*reinterpret_cast<float4 *>(hn + (size_t)r * W + n) = make_float4(
+		    hh.x + fmaxf(v.x, 0.f), hh.y + fmaxf(v.y, 0.f), hh.z + fmaxf(v.z, 0.f), hh.w + fmaxf(v.w, 0.f));
+	}
+	__device__ void operator()(int r, int n, float z0, float z1, float2 hh) const
 	{
 		const float2 v = make_float2(z0 + bias[n], z1 + bias[n + 1]);
-		const float2 hh = *reinterpret_cast<const float2 *>(h + (size_t)r * W + n);
 		*reinterpret_cast<float2 *>(pre + (size_t)r * W + n) = v;
 		*reinterpret_cast<float2 *>(hn + (size_t)r * W + n) = make_float2(hh.x + fmaxf(v.x, 0.f), hh.y + fmaxf(v.y, 0.f));
 	}
@@ -245,27 +240,49 @@ struct EUpdate {  // hn = h + relu(Z + bu), pre = Z + bu
 
 struct ESplit {  // input gradient of the node update [d h | d a]: dh += the first W columns, da stored
 	float *dh, *da;   // da: row stride 2 W, columns W..2W-1 hold d a
-	__device__ void operator()(int r, int n, float z0, float z1) const
+	__device__ float2 old(int r, int n) const
 	{
-		if (n < W) {
-			float2 *o = reinterpret_cast<float2 *>(dh + (size_t)r * W + n);
-			const float2 v = *o;
-			*o = make_float2(v.x + z0, v.y + z1);
-		} else {
-			*reinterpret_cast<float2 *>(da + (size_t)r * 2 * W + n) = make_float2(z0, z1);
-		}
+		return n < W ? *reinterpret_cast<const float2 *>(dh + (size_t)r * W + n) : make_float2(0.f, 0.f);
+	}
+	__device__ void operator()(int r, int n, float z0, float z1, float2 v) const
+	{
+		if (n < W) *reinterpret_cast<float2 *>(dh + (size_t)r * W + n) = make_float2(v.x + z0, v.y + z1);
+		else *reinterpret_cast<float2 *>(da + (size_t)r * 2 * W + n) = make_float2(z0, z1);
 	}
 };
 struct EAccum {  // out += Z (row stride ldo)
 	float *out;
 	int ldo;
-	__device__ void operator()(int r, int n, float z0, float z1) const
+	__device__ float2 old(int r, int n) const { return *reinterpret_cast<const float2 *>(out + (size_t)r * ldo + n); }
+	__device__ void operator()(int r, int n, float z0, float z1, float2 v) const
 	{
-		float2 *o = reinterpret_cast<float2 *>(out + (size_t)r * ldo + n);
-		const float2 v = *o;
-		*o = make_float2(v.x + z0, v.y + z1);
+		*reinterpret_cast<float2 *>(out + (size_t)r * ldo + n) = make_float2(v.x + z0, v.y + z1);
 	}
 };
+
+/* a tile's old values (epilogue inputs) for this thread's output positions */
+template <int N, class E>
+__device__ __forceinline__ void tile_old(const E &ep, int row0, int rows, float2 (*old)[2])
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	for (int nt = 0; nt < N / 8; nt++)
+		for (int hh = 0; hh < 2; hh++) {
+			const int r = row0 + warp * 16 + g + 8 * hh;
+			old[nt][hh] = r < rows ? ep.old(r, nt * 8 + 2 * t) : make_float2(0.f, 0.f);
+		}
+}
+
+template <int N, class E>
+__device__ __forceinline__ void tile_epilogue(const E &ep, int row0, int rows, const float (*c)[4],
+                                              const float2 (*old)[2])
+{
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+	for (int nt = 0; nt < N / 8; nt++)
+		for (int hh = 0; hh < 2; hh++) {
+			const int r = row0 + warp * 16 + g + 8 * hh;
+			if (r < rows) ep(r, nt * 8 + 2 * t, c[nt][2 * hh], c[nt][2 * hh + 1], old[nt][hh]);
+		}
+}
 
 // ------------------------------------ kernels ------------------------------------
 /* Z = A W^T over persistent 64-row tiles: the CTA stages its weight operand once
@@ -286,19 +303,15 @@ __global__ void __launch_bounds__(GT) k_gemm(int rows, L ld, const float *w, int
 			sB[n * (K + 8) + k] = __float2bfloat16_rn((n < nvalid && k < kvalid) ? w[(size_t)k * ldw + n] : 0.f);
 		}
 	}
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 	for (int row0 = blockIdx.x * GR; row0 < rows; row0 += gridDim.x * GR) {
 		__syncthreads();  // the previous tile's operands are consumed
 		stage_rows<K>(ld, row0, rows, ri, sA);
 		__syncthreads();
+		float2 old[N / 8][2];
+		tile_old<N>(ep, row0, rows, old);
 		float c[N / 8][4];
 		tile_mma<K, N>(sA, sB, c);
-		for (int nt = 0; nt < N / 8; nt++)
-			for (int hh = 0; hh < 2; hh++) {
-				const int r = row0 + warp * 16 + g + 8 * hh;
-				if (r >= rows) continue;
-				ep(r, nt * 8 + 2 * t, c[nt][2 * hh], c[nt][2 * hh + 1]);
-			}
+		tile_epilogue<N>(ep, row0, rows, c, old);
 	}
 }
 
@@ -389,6 +402,363 @@ __global__ void __launch_bounds__(GT) k_wgrad(int rows, XL xl, ZL zl, float *par
 		}
 		reinterpret_cast<float4 *>(bpart + (size_t)blockIdx.x * N)[threadIdx.x] = s;
 	}
+}
+
+/* ------------------------- GEMMs with bulk-copied operands -------------------------
+ * Row operands that are whole contiguous FP32 row blocks are staged by bulk
+ * copies (cp.async.bulk, the TMA engine) into a ring of NST tile buffers per
+ * CTA: while the CTA converts one tile to BF16 and multiplies it, the copies
+ * of its next tiles are in flight.  BRows<WA, WB, MODE>: rows of a (WA
+ * columns) and, when WB > 0, rows of b (WB columns), both with row stride
+ * equal to their width; MODE 0 gives the operand [a | b] (K = WA + WB), MODE 1
+ * gives a where b > 0 (WB == WA, K = WA; the ReLU mask of a backward pass). */
+constexpr int NST = 2;  // staged tiles per CTA
+
+template <int WA, int WB, int MODE>
+struct BRows {
+	const float *a, *b;
+	static constexpr int K = MODE == 0 ? WA + WB : WA;
+	static constexpr int FLOATS = GR * (WA + WB);  // one staged tile
+	static_assert(MODE == 0 || WA == WB, "a mask has the operand's width");
+	__device__ unsigned bytes(int nr) const { return (unsigned)nr * (WA + WB) * 4u; }
+	__device__ void copy(float *st, int row0, int nr, uint64_t *bar) const
+	{
+		bulk_g2s(st, a + (size_t)row0 * WA, (unsigned)nr * WA * 4u, bar);
+		if (WB > 0) bulk_g2s(st + GR * WA, b + (size_t)row0 * WB, (unsigned)nr * WB * 4u, bar);
+	}
+	__device__ float4 quad(const float *st, int rr, int q) const
+	{
+		if (MODE == 1) {
+			const float4 d = reinterpret_cast<const float4 *>(st + rr * WA)[q];
+			const float4 z = reinterpret_cast<const float4 *>(st + GR * WA + rr * WA)[q];
+			return make_float4(z.x > 0.f ? d.x : 0.f, z.y > 0.f ? d.y : 0.f, z.z > 0.f ? d.z : 0.f,
+			                   z.w > 0.f ? d.w : 0.f);
+		}
+		if (WB == 0 || q < WA / 4) return reinterpret_cast<const float4 *>(st + rr * WA)[q];
+		return reinterpret_cast<const float4 *>(st + GR * WA + rr * WB)[q - WA / 4];
+	}
+};
+
+/* number of the CTA's tiles blockIdx.x + i gridDim.x below ntiles */
+__device__ __forceinline__ int local_tiles(int ntiles)
+{
+	return (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+}
+
+/* thread 0: the copies of the CTA's local tile i into ring slot i mod NST */
+template <class X, class Z>
+__device__ __forceinline__ void issue_tile(const X &x, const Z *z, int rows, int i, float *stg, uint64_t *bar)
+{
+	const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * GR, nr = min(GR, rows - row0);
+	float *st = stg + (size_t)s * (X::FLOATS + (z ? Z::FLOATS : 0));
+	mbar_arrive_expect_tx(&bar[s], x.bytes(nr) + (z ? z->bytes(nr) : 0u));
+	x.copy(st, row0, nr, &bar[s]);
+	if (z) z->copy(st + X::FLOATS, row0, nr, &bar[s]);
+}
+
+/* after a wait ran out: thread 0 waits (bounded) for the copies still in
+ * flight into the ring, from local tile i on, and records the error */
+__device__ __forceinline__ void abort_ring(int i, int nloc, uint64_t *bar, int *err)
+{
+	if (threadIdx.x != 0) return;
+	for (int j = i; j < nloc && j < i + NST; j++) mbar_wait_bounded(&bar[j % NST], (j / NST) & 1, 200000000LL);
+	atomicExch(err, 1);
+}
+
+/* k_gemm with the row operand staged by bulk copies (the weights as in k_gemm) */
+template <int K, int N, bool TRANS, class BL, class E>
+__global__ void __launch_bounds__(GT) k_gemm_bulk(int rows, BL bl, const float *w, int ldw, int nvalid, int kvalid,
+                                                   E ep, int *err)
+{
+	static_assert(BL::K == K, "operand width");
+	extern __shared__ __align__(128) unsigned char smem[];
+	float *stg = reinterpret_cast<float *>(smem);                                   // [NST][BL::FLOATS]
+	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(stg + NST * BL::FLOATS);  // [64][K + 8]
+	__nv_bfloat16 *sB = sA + GR * (K + 8);                                          // [N][K + 8]
+	__shared__ __align__(8) uint64_t bar[NST];
+	__shared__ int abort_;
+	const int nloc = local_tiles((rows + GR - 1) / GR);
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < NST; s++) mbar_init(&bar[s], 1);
+		abort_ = 0;
+		mbar_init_fence();
+	}
+	__syncthreads();
+	if (threadIdx.x == 0)
+		for (int i = 0; i < NST && i < nloc; i++) issue_tile<BL, BL>(bl, nullptr, rows, i, stg, bar);
+	if (!TRANS) {
+		stage_w<K, N>(w, ldw, nvalid, kvalid, sB);
+	} else {
+		for (int e = threadIdx.x; e < N * K; e += GT) {
+			const int k = e / N, n = e - k * N;
+			sB[n * (K + 8) + k] = __float2bfloat16_rn((n < nvalid && k < kvalid) ? w[(size_t)k * ldw + n] : 0.f);
+		}
+	}
+	for (int i = 0; i < nloc; i++) {
+		const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * GR, nr = min(GR, rows - row0);
+		if (!mbar_wait_bounded(&bar[s], (i / NST) & 1)) abort_ = 1;
+		const float *st = stg + (size_t)s * BL::FLOATS;
+		for (int e = threadIdx.x; e < GR * (K / 4); e += GT) {
+			const int rr = e / (K / 4), q = e - rr * (K / 4);
+			const float4 v = rr < nr ? bl.quad(st, rr, q) : make_float4(0.f, 0.f, 0.f, 0.f);
+			*reinterpret_cast<uint2 *>(sA + rr * (K + 8) + 4 * q) = make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
+		}
+		fence_proxy_async_smem();  // this thread's reads of the slot before the copy that refills it
+		__syncthreads();           // sA (and at i = 0 sB) ready; the slot is free
+		if (abort_) { abort_ring(i, nloc, bar, err); return; }
+		if (threadIdx.x == 0 && i + NST < nloc) issue_tile<BL, BL>(bl, nullptr, rows, i + NST, stg, bar);
+		float2 old[N / 8][2];
+		tile_old<N>(ep, row0, rows, old);
+		float c[N / 8][4];
+		tile_mma<K, N>(sA, sB, c);
+		tile_epilogue<N>(ep, row0, rows, c, old);
+		__syncthreads();  // sA consumed
+	}
+}
+
+/* k_wgrad with both operands staged by bulk copies (one ring slot holds the
+ * X and the dZ rows of a chunk) */
+template <int K, int N, class XL, class ZL>
+__global__ void __launch_bounds__(GT) k_wgrad_bulk(int rows, XL xl, ZL zl, float *part, float *bpart, int *err)
+{
+	static_assert(XL::K == K && ZL::K == N, "operand widths");
+	static_assert(GT % (N / 4) == 0, "a thread stages the same column quad of dZ in every row");
+	constexpr int SLOT = XL::FLOATS + ZL::FLOATS;
+	extern __shared__ __align__(128) unsigned char smem[];
+	float *stg = reinterpret_cast<float *>(smem);                                // [NST][SLOT]
+	__nv_bfloat16 *sZ = reinterpret_cast<__nv_bfloat16 *>(stg + NST * SLOT);    // [64][N + 8]
+	__nv_bfloat16 *sX = sZ + GR * (N + 8);                                       // [64][K + 8]
+	__shared__ __align__(8) uint64_t bar[NST];
+	__shared__ float4 sbias[GT];
+	__shared__ int abort_;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int nloc = local_tiles((rows + GR - 1) / GR);
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < NST; s++) mbar_init(&bar[s], 1);
+		abort_ = 0;
+		mbar_init_fence();
+	}
+	__syncthreads();
+	if (threadIdx.x == 0)
+		for (int i = 0; i < NST && i < nloc; i++) issue_tile(xl, &zl, rows, i, stg, bar);
+	float c[K / 8][4];
+	for (int nt = 0; nt < K / 8; nt++)
+		for (int q = 0; q < 4; q++) c[nt][q] = 0.f;
+	float4 bsum = make_float4(0.f, 0.f, 0.f, 0.f);
+	const int mi = lane >> 3, mr = lane & 7;
+	for (int i = 0; i < nloc; i++) {
+		const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * GR, nr = min(GR, rows - row0);
+		if (!mbar_wait_bounded(&bar[s], (i / NST) & 1)) abort_ = 1;
+		const float *st = stg + (size_t)s * SLOT;
+		for (int e = threadIdx.x; e < GR * (K / 4); e += GT) {
+			const int rr = e / (K / 4), q = e - rr * (K / 4);
+			const float4 v = rr < nr ? xl.quad(st, rr, q) : make_float4(0.f, 0.f, 0.f, 0.f);
+			*reinterpret_cast<uint2 *>(sX + rr * (K + 8) + 4 * q) = make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
+		}
+		for (int e = threadIdx.x; e < GR * (N / 4); e += GT) {
+			const int rr = e / (N / 4), q = e - rr * (N / 4);
+			const float4 v = rr < nr ? zl.quad(st + XL::FLOATS, rr, q) : make_float4(0.f, 0.f, 0.f, 0.f);
+			bsum.x += v.x; bsum.y += v.y; bsum.z += v.z; bsum.w += v.w;
+			*reinterpret_cast<uint2 *>(sZ + rr * (N + 8) + 4 * q) = make_uint2(pack_bf16(v.x, v.y), pack_bf16(v.z, v.w));
+		}
+		fence_proxy_async_smem();
+		__syncthreads();
+		if (abort_) { abort_ring(i, nloc, bar, err); return; }
+		if (threadIdx.x == 0 && i + NST < nloc) issue_tile(xl, &zl, rows, i + NST, stg, bar);
+		if (warp * 16 < N) {
+			for (int k0 = 0; k0 < GR; k0 += 16) {
+				unsigned af[4];
+				ldsm_x4_trans(af, sZ + (k0 + mr + ((mi & 2) ? 8 : 0)) * (N + 8) + warp * 16 + ((mi & 1) ? 8 : 0));
+				for (int nt = 0; nt < K / 8; nt += 2) {
+					unsigned bf[4];
+					ldsm_x4_trans(bf, sX + (k0 + mr + ((mi & 1) ? 8 : 0)) * (K + 8) + nt * 8 + ((mi & 2) ? 8 : 0));
+					mma_bf16(c[nt], af, bf);
+					mma_bf16(c[nt + 1], af, bf + 2);
+				}
+			}
+		}
+		__syncthreads();  // sX, sZ consumed
+	}
+	const int g = lane >> 2, t = lane & 3;
+	if (warp * 16 < N) {
+		float *pc = part + (size_t)blockIdx.x * N * K;
+		for (int nt = 0; nt < K / 8; nt++)
+			for (int hh = 0; hh < 2; hh++)
+				for (int j = 0; j < 2; j++) pc[(size_t)(warp * 16 + g + 8 * hh) * K + nt * 8 + 2 * t + j] = c[nt][2 * hh + j];
+	}
+	sbias[threadIdx.x] = bsum;
+	__syncthreads();
+	if (threadIdx.x < N / 4) {
+		float4 sb = make_float4(0.f, 0.f, 0.f, 0.f);
+		for (int j = threadIdx.x; j < GT; j += N / 4) {
+			sb.x += sbias[j].x; sb.y += sbias[j].y; sb.z += sbias[j].z; sb.w += sbias[j].w;
+		}
+		reinterpret_cast<float4 *>(bpart + (size_t)blockIdx.x * N)[threadIdx.x] = sb;
+	}
+}
+
+/* ------------------------ GEMMs on the fifth-generation tensor cores ------------------------
+ * k_gemm_tc: Z = A W^T (+ epilogue) over 128-row tiles, one CTA of four warps
+ * per tile at a time, persistent over its tiles.  The row operand arrives by
+ * per-row bulk copies into a ring of NST padded FP32 tiles (row stride width + 4
+ * floats: the conversion reads are free of bank conflicts); every thread
+ * converts its own row to BF16 into the no-swizzle K-major core-matrix layout;
+ * one thread issues the tile's K / 16 tcgen05.mma (M = 128) into a tensor-
+ * memory accumulator of N FP32 columns and commits them to an mbarrier; each
+ * thread then reads its row of the accumulator (tcgen05.ld 32x32b) and runs
+ * the epilogue on it, four columns at a time.  The epilogue's inputs are
+ * loaded while the MMAs run.  Every wait is bounded: one that runs out sets
+ * the error word, and the CTA ends once its copies and MMAs are done and its
+ * tensor memory is freed.
+ * Measured on the 16 x 13,156-row node update: 129-148 us against 79 us for
+ * k_gemm_bulk with mma.sync.  The GEMM moves rows (42 FLOP per FP32 byte) and
+ * this kernel's 188 KB of shared memory leaves one CTA of four warps per SM,
+ * each tile's steps in sequence; the mma.sync kernel runs two to three CTAs per
+ * SM.  So mma.sync is the default path (fv_mpnn_set_gemm_path). */
+constexpr int TM = 128;  // rows per tensor-core tile (one per thread)
+
+/* [a | b] rows (WA, WB columns; b absent when WB == 0) copied row by row into
+ * padded tile rows */
+template <int WA, int WB>
+struct PRows {
+	const float *a, *b;
+	static constexpr int K = WA + WB;
+	static constexpr int PA = WA + 4, PB = WB > 0 ? WB + 4 : 0;  // padded row strides (floats)
+	static constexpr int FLOATS = TM * (PA + PB);
+	__device__ unsigned bytes(int nr) const { return (unsigned)nr * (WA + WB) * 4u; }
+	/* warp-wide: lane l copies rows l, l + 32, ... of a, then of b */
+	__device__ void copy_rows(float *st, int row0, int nr, uint64_t *bar, int lane) const
+	{
+		for (int j = lane; j < nr; j += 32) bulk_g2s(st + j * PA, a + (size_t)(row0 + j) * WA, WA * 4u, bar);
+		if (WB > 0)
+			for (int j = lane; j < nr; j += 32)
+				bulk_g2s(st + TM * PA + j * PB, b + (size_t)(row0 + j) * WB, WB * 4u, bar);
+	}
+	/* columns 8 kc .. 8 kc + 7 of tile row m */
+	__device__ void read8(const float *st, int m, int kc, float4 &lo, float4 &hi) const
+	{
+		const float *p = 8 * kc < WA ? st + m * PA + 8 * kc : st + TM * PA + m * PB + (8 * kc - WA);
+		lo = reinterpret_cast<const float4 *>(p)[0];
+		hi = reinterpret_cast<const float4 *>(p)[1];
+	}
+};
+
+template <int K, int N, class PL, class E>
+__global__ void __launch_bounds__(GT) k_gemm_tc(int rows, PL pl, const float *w, int ldw, int nvalid, int kvalid,
+                                                 E ep, int *err)
+{
+	static_assert(PL::K == K && K % 16 == 0 && N % 16 == 0 && N >= 32 && N <= 256 && GT == TM, "tile shape");
+	constexpr unsigned LBO_A = TM * 16, LBO_B = N * 16;  // bytes between K-chunks (8-row groups adjacent)
+	constexpr uint32_t IDESC = tc_idesc_bf16(TM, N);
+	extern __shared__ __align__(128) unsigned char smem[];
+	unsigned char *sA = smem;                                           // [K / 8][TM][16 B]
+	unsigned char *sB = sA + (size_t)TM * K * 2;                        // [K / 8][N][16 B]
+	float *stg = reinterpret_cast<float *>(sB + (size_t)N * K * 2);     // [NST][PL::FLOATS]
+	__shared__ __align__(8) uint64_t bar[NST];
+	__shared__ __align__(8) uint64_t mma_bar;
+	__shared__ uint32_t tmem_slot;
+	// a copy wait that ran out (read after the conversion barrier), an MMA wait that ran out
+	// (read after the tile's last barrier): two flags, so no write races with the other read
+	__shared__ int abort_copy, abort_mma;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, m = threadIdx.x;
+	const int ntiles = (rows + TM - 1) / TM;
+	const int nloc = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+	if (warp == 0) tc_alloc(&tmem_slot, N);
+	if (threadIdx.x == 0) {
+		for (int s = 0; s < NST; s++) mbar_init(&bar[s], 1);
+		mbar_init(&mma_bar, 1);
+		abort_copy = 0;
+		abort_mma = 0;
+		mbar_init_fence();
+	}
+	tc_fence_before_sync();
+	__syncthreads();
+	tc_fence_after_sync();
+	const uint32_t tmem = tmem_slot;
+	auto issue = [&](int i) {  // warp 0: the copies of local tile i into ring slot i mod NST
+		const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * TM, nr = min(TM, rows - row0);
+		if (lane == 0) mbar_arrive_expect_tx(&bar[s], pl.bytes(nr));
+		__syncwarp();
+		pl.copy_rows(stg + (size_t)s * PL::FLOATS, row0, nr, &bar[s], lane);
+	};
+	if (warp == 0)
+		for (int i = 0; i < NST && i < nloc; i++) issue(i);
+	// weights W [N][K] (row stride ldw) as BF16 core matrices, once per CTA
+	for (int e = threadIdx.x; e < N * (K / 8); e += GT) {
+		const int n = e % N, kc = e / N;
+		unsigned q[4];
+		for (int j = 0; j < 4; j++) {
+			const int k = 8 * kc + 2 * j;
+			const float x0 = (n < nvalid && k < kvalid) ? w[(size_t)n * ldw + k] : 0.f;
+			const float x1 = (n < nvalid && k + 1 < kvalid) ? w[(size_t)n * ldw + k + 1] : 0.f;
+			q[j] = pack_bf16(x0, x1);
+		}
+		*reinterpret_cast<uint4 *>(sB + (size_t)kc * LBO_B + n * 16) = make_uint4(q[0], q[1], q[2], q[3]);
+	}
+	const unsigned aaddr = smem_u32(sA), baddr = smem_u32(sB);
+	int i = 0;
+	for (; i < nloc; i++) {
+		const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * TM, nr = min(TM, rows - row0);
+		if (!mbar_wait_bounded(&bar[s], (i / NST) & 1)) abort_copy = 1;
+		const float *st = stg + (size_t)s * PL::FLOATS;
+		for (int kc = 0; kc < K / 8; kc++) {
+			float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+			if (m < nr) pl.read8(st, m, kc, lo, hi);
+			*reinterpret_cast<uint4 *>(sA + (size_t)kc * LBO_A + m * 16) =
+			    make_uint4(pack_bf16(lo.x, lo.y), pack_bf16(lo.z, lo.w), pack_bf16(hi.x, hi.y), pack_bf16(hi.z, hi.w));
+		}
+		fence_proxy_async_smem();  // the BF16 tile (and at i = 0 the weights) to the tensor cores; the slot's reads
+		__syncthreads();
+		if (abort_copy) break;
+		if (warp == 0 && i + NST < nloc) issue(i + NST);
+		if (threadIdx.x == 0) {
+			tc_fence_after_sync();
+			for (int kk = 0; kk < K / 16; kk++)
+				tc_mma_bf16(tmem, tc_sdesc(aaddr + kk * 2 * LBO_A, LBO_A, 128), tc_sdesc(baddr + kk * 2 * LBO_B, LBO_B, 128),
+				            IDESC, kk > 0);
+			tc_commit(&mma_bar);
+		}
+		// The epilogue goes through shared memory (sA is free once the MMAs have completed):
+		// each warp turns its 32 rows x 16 columns of the accumulator into pieces of 8 rows x
+		// 64 bytes, so the epilogue's loads and stores are coalesced.  Its inputs are loaded
+		// in the same pattern while the MMAs run.
+		float *xp = reinterpret_cast<float *>(sA) + warp * 32 * 20;  // [32][20] per warp
+		const int er = lane >> 2, ec = 4 * (lane & 3);               // row in an 8-row piece, column quad
+		float4 old[N / 16][4];
+		for (int cc = 0; cc < N / 16; cc++)
+			for (int j = 0; j < 4; j++) {
+				const int rr = warp * 32 + 8 * j + er;
+				old[cc][j] = rr < nr ? ep.old4(row0 + rr, 16 * cc + ec) : make_float4(0.f, 0.f, 0.f, 0.f);
+			}
+		if (!mbar_wait_bounded(&mma_bar, i & 1)) abort_mma = 1;
+		tc_fence_after_sync();
+		for (int cc = 0; cc < N / 16; cc++) {
+			float v[16];
+			tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(16 * cc), v);
+			for (int q = 0; q < 4; q++)
+				reinterpret_cast<float4 *>(xp + lane * 20)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+			__syncwarp();
+			for (int j = 0; j < 4; j++) {
+				const int rr = warp * 32 + 8 * j + er;
+				const float4 z = *reinterpret_cast<const float4 *>(xp + (8 * j + er) * 20 + ec);
+				if (rr < nr) ep.put4(row0 + rr, 16 * cc + ec, z, old[cc][j]);
+			}
+			__syncwarp();
+		}
+		tc_fence_before_sync();
+		__syncthreads();  // sA and the accumulator free for the next tile
+		if (abort_mma) { i++; break; }
+	}
+	if ((abort_copy || abort_mma) && threadIdx.x == 0) {
+		// copies still in flight into the ring (tiles from the one waited on), and the last MMAs
+		for (int j = i; j < nloc && j < i + NST; j++) mbar_wait_bounded(&bar[j % NST], (j / NST) & 1, 200000000LL);
+		mbar_wait_bounded(&mma_bar, (i - 1) & 1, 200000000LL);
+		atomicExch(err, 1);
+	}
+	tc_fence_before_sync();
+	__syncthreads();
+	tc_fence_after_sync();
+	if (warp == 0) tc_dealloc(tmem, N);
 }
 
 /* sum of the CTA partials of the valid [nv][kv] part of the padded [N][K]
@@ -663,6 +1033,8 @@ struct fv_mpnn {
 	float *y = nullptr, *dy = nullptr, *cond = nullptr, *uinf = nullptr, *t2 = nullptr, *dh = nullptr;
 	float *pc = nullptr, *sgrad = nullptr, *wst = nullptr, *epart = nullptr;
 	float *part = nullptr, *bpart = nullptr, *rtmp = nullptr, *lpart = nullptr;
+	int *err = nullptr;  // set by a kernel whose bulk-copy or MMA wait ran out of time
+	int gemm_path = 1;   // forward cell GEMMs: 0 tcgen05, 1 mma.sync (faster here: see k_gemm_tc)
 	std::vector<void *> owned;
 };
 
@@ -744,6 +1116,40 @@ void gemm(size_t rows, L ld, const float *w, int ldw, int nvalid, int kvalid, E 
 	k_gemm<K, Nn, TRANS, L, E><<<gemm_grid(rows), GT, sm, s>>>((int)rows, ld, w, ldw, nvalid, kvalid, ep);
 }
 
+/* CTAs of kern resident at once on the current device (dynamic shared memory
+ * smem), at most cap; raises the kernel's dynamic shared-memory limit first */
+template <class F>
+unsigned resident_grid(F *kern, size_t smem, size_t work, unsigned cap)
+{
+	int dev = 0, sms = 0, per = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, GT, smem);
+	const size_t n = std::min<size_t>({work, (size_t)std::max(per, 1) * std::max(sms, 1), (size_t)cap});
+	return (unsigned)std::max<size_t>(n, 1);
+}
+
+/* gemm on the fifth-generation tensor cores (k_gemm_tc; rows of PRows) */
+template <int K, int Nn, class PL, class E>
+void gemm_tc(fv_mpnn *N, size_t rows, PL pl, const float *w, int ldw, int nvalid, int kvalid, E ep, cudaStream_t s)
+{
+	const size_t sm = sizeof(__nv_bfloat16) * (size_t)(TM + Nn) * K + sizeof(float) * NST * PL::FLOATS;
+	auto *kern = k_gemm_tc<K, Nn, PL, E>;
+	const unsigned grid = resident_grid(kern, sm, nb(rows, TM), 4 * 152);
+	kern<<<grid, GT, sm, s>>>((int)rows, pl, w, ldw, nvalid, kvalid, ep, N->err);
+}
+
+/* gemm with the row operand staged by bulk copies (BRows) */
+template <int K, int Nn, bool TRANS, class BL, class E>
+void gemm_bulk(fv_mpnn *N, size_t rows, BL bl, const float *w, int ldw, int nvalid, int kvalid, E ep, cudaStream_t s)
+{
+	const size_t sm = sizeof(float) * NST * BL::FLOATS + sizeof(__nv_bfloat16) * (GR + Nn) * (K + 8);
+	auto *kern = k_gemm_bulk<K, Nn, TRANS, BL, E>;
+	const unsigned grid = resident_grid(kern, sm, nb(rows, GR), 4 * 152);
+	kern<<<grid, GT, sm, s>>>((int)rows, bl, w, ldw, nvalid, kvalid, ep, N->err);
+}
+
 /* forward pass for B members; activations kept for the backward pass */
 cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
 {
@@ -759,16 +1165,18 @@ cudaError_t forward(fv_mpnn *N, int B, cudaStream_t s)
 		// Zm = pc_s[src] + pc_d[dst] + W_e e + bm
 		float *wst = N->wst + (size_t)l * 2 * W * W;
 		k_stack_w<<<nb(2 * W * W, 256), 256, 0, s>>>(P + Y.wm[l], wst);
-		gemm<W, 2 * W, false>(rows_c, LRows{hl, W, W}, wst, W, 2 * W, W, EStore{nullptr, N->pc, nullptr, 2 * W, 2 * W, 0},
-		                      s);
+		const EStore pc_ep{nullptr, N->pc, nullptr, 2 * W, 2 * W, 0};
+		if (N->gemm_path == 0) gemm_tc<W, 2 * W>(N, rows_c, PRows<W, 0>{hl, nullptr}, wst, W, 2 * W, W, pc_ep, s);
+		else gemm_bulk<W, 2 * W, false>(N, rows_c, BRows<W, 0, 0>{hl, nullptr}, wst, W, 2 * W, W, pc_ep, s);
 		k_msg_fwd<<<nb(rows_m, MROWS), 256, 0, s>>>(G, B, N->pc, P + Y.wm[l], P + Y.bm[l], mp);
 		float *al = N->agg + l * rows_c * W;
 		k_aggregate<<<nb(rows_c, MROWS), 256, 0, s>>>(G, B, mp, al);
-		gemm<KUPD, W, false>(rows_c, LUpd{hl, al}, P + Y.wu[l], KUPD, W, KUPD,
-		                     EUpdate{P + Y.bu[l], hl, N->h + (l + 1) * rows_c * W, N->upre + l * rows_c * W}, s);
+		const EUpdate up_ep{P + Y.bu[l], hl, N->h + (l + 1) * rows_c * W, N->upre + l * rows_c * W};
+		if (N->gemm_path == 0) gemm_tc<KUPD, W>(N, rows_c, PRows<W, W>{hl, al}, P + Y.wu[l], KUPD, W, KUPD, up_ep, s);
+		else gemm_bulk<KUPD, W, false>(N, rows_c, BRows<W, W, 0>{hl, al}, P + Y.wu[l], KUPD, W, KUPD, up_ep, s);
 	}
-	gemm<W, NDEC, false>(rows_c, LRows{N->h + Y.layers * rows_c * W, W, W}, P + Y.wd, W, 4, W,
-	                     EStore{P + Y.bd, N->y, nullptr, 4, 4, 0}, s);
+	gemm_bulk<W, NDEC, false>(N, rows_c, BRows<W, 0, 0>{N->h + Y.layers * rows_c * W, nullptr}, P + Y.wd, W, 4, W,
+	                          EStore{P + Y.bd, N->y, nullptr, 4, 4, 0}, s);
 	count_launches(2 + 5 * Y.layers);
 	return cudaGetLastError();
 }
@@ -782,6 +1190,22 @@ void wgrad(fv_mpnn *N, size_t rows, XL xl, ZL zl, int nv, int kv, float *gw, flo
 	const unsigned ctas = std::min<unsigned>(nb(rows, GR), kWgradCtas);
 	const size_t sm = sizeof(__nv_bfloat16) * GR * (Nn + 8 + K + 8);
 	k_wgrad<K, Nn, XL, ZL><<<ctas, GT, sm, s>>>((int)rows, xl, zl, N->part, N->bpart);
+	const int nw = nv * kv;
+	k_reduce_parts<<<dim3(nb(nw + nv, 256), kReduceSlices), 256, 0, s>>>((int)ctas, Nn, K, nv, kv, N->part, N->bpart,
+	                                                                   N->rtmp);
+	k_reduce_final<<<nb(nw + nv, 256), 256, 0, s>>>(kReduceSlices, nw, nv, kv, N->rtmp, gw, gb, stacked, 2 * W + 3);
+	count_launches(3);
+}
+
+/* wgrad with both operands staged by bulk copies (BRows) */
+template <int K, int Nn, class XL, class ZL>
+void wgrad_bulk(fv_mpnn *N, size_t rows, XL xl, ZL zl, int nv, int kv, float *gw, float *gb, cudaStream_t s,
+                int stacked = 0)
+{
+	const size_t sm = sizeof(float) * NST * (XL::FLOATS + ZL::FLOATS) + sizeof(__nv_bfloat16) * GR * (Nn + 8 + K + 8);
+	auto *kern = k_wgrad_bulk<K, Nn, XL, ZL>;
+	const unsigned ctas = resident_grid(kern, sm, nb(rows, GR), kWgradCtas);
+	kern<<<ctas, GT, sm, s>>>((int)rows, xl, zl, N->part, N->bpart, N->err);
 	const int nw = nv * kv;
 	k_reduce_parts<<<dim3(nb(nw + nv, 256), kReduceSlices), 256, 0, s>>>((int)ctas, Nn, K, nv, kv, N->part, N->bpart,
 	                                                                   N->rtmp);
@@ -807,20 +1231,24 @@ cudaError_t backward(fv_mpnn *N, int B, cudaStream_t s)
 		const float *al = N->agg + l * rows_c * W;
 		const float *up = N->upre + l * rows_c * W, *mp = N->mpre + l * rows_m * W;
 		// update: hn = h + relu(Zu), Zu = Wu [h, a] + bu;  dZu = dh (Zu > 0)
-		wgrad<KUPD, W>(N, rows_c, LUpd{hl, al}, LRelu{N->dh, up}, W, KUPD, Gr + Y.wu[l], Gr + Y.bu[l], s);
+		wgrad_bulk<KUPD, W>(N, rows_c, BRows<W, W, 0>{hl, al}, BRows<W, W, 1>{N->dh, up}, W, KUPD, Gr + Y.wu[l],
+		                    Gr + Y.bu[l], s);
 		// dh (residual path) += the update's d[h] columns; d[a] into t2 (columns W..2W-1).
 		// Each CTA reads and then updates only its own rows of dh.
-		gemm<W, KUPD, true>(rows_c, LRelu{N->dh, up}, P + Y.wu[l], KUPD, KUPD, W, ESplit{N->dh, N->t2}, s);
+		gemm_bulk<W, KUPD, true>(N, rows_c, BRows<W, W, 1>{N->dh, up}, P + Y.wu[l], KUPD, KUPD, W,
+		                         ESplit{N->dh, N->t2}, s);
 		// messages: dZm = d[a] of the destination, masked by Zm > 0, summed per cell over
 		// outgoing (S_out) and incoming (S_in) messages; the first layer's weight and input
 		// gradients are cell-level GEMMs of S = [S_out, S_in]
 		const unsigned mb = std::min<unsigned>(nb(rows_c, MROWS), kMsgBackBlocks);
 		k_msg_back<<<mb, 256, 0, s>>>(G, B, mp, N->t2, KUPD, W, N->sgrad, N->epart);
 		k_reduce_edge<<<4 * W, 128, 0, s>>>((int)mb, N->epart, Gr + Y.wm[l], Gr + Y.bm[l]);
+		// (plain loads: one CTA per SM fits the bulk ring of this pair, which ran slower)
 		wgrad<2 * W, W>(N, rows_c, LRows{N->sgrad, 2 * W, 2 * W}, LRows{hl, W, W}, W, 2 * W, Gr + Y.wm[l], nullptr, s,
 		                1);
 		const float *wst = N->wst + (size_t)l * 2 * W * W;
-		gemm<2 * W, W, true>(rows_c, LRows{N->sgrad, 2 * W, 2 * W}, wst, W, W, 2 * W, EAccum{N->dh, W}, s);
+		gemm_bulk<2 * W, W, true>(N, rows_c, BRows<2 * W, 0, 0>{N->sgrad, nullptr}, wst, W, W, 2 * W, EAccum{N->dh, W},
+		                          s);
 		count_launches(4);
 	}
 	// encoder: h0 = relu(We x + be)
@@ -854,6 +1282,20 @@ cudaError_t upload_conditions(fv_mpnn *N, const fv_physics_cfg *phys, int B, cud
 	if (!e) e = cudaMemcpyAsync(N->uinf, uinf.data(), sizeof(float) * uinf.size(), cudaMemcpyHostToDevice, s);
 	if (!e) e = cudaStreamSynchronize(s);  // host vectors go out of scope
 	return e;
+}
+
+/* status of a synchronised call: a kernel whose bulk-copy wait ran out of
+ * time left its error word set (cleared here) */
+fv_status finish(fv_mpnn *N, cudaError_t e, const char *what)
+{
+	int timed_out = 0;
+	if (!e) e = cudaMemcpy(&timed_out, N->err, sizeof(int), cudaMemcpyDeviceToHost);
+	if (!e && timed_out) {
+		cudaMemset(N->err, 0, sizeof(int));
+		set_error(std::string(what) + ": a bulk-copy or MMA wait of a GEMM ran out of time");
+		return FV_ERR_CUDA;
+	}
+	return cuda_status(e, what);
 }
 
 }  // namespace
@@ -937,6 +1379,7 @@ fv_status fv_mpnn_create(fv_mesh *m, int layers, const int *wall_markers, int nw
 	up(&N->g, z); up(&N->m1, z); up(&N->m2, z);
 	std::vector<float> sc(N->scale_h, N->scale_h + 4);
 	up(&N->scale, sc);
+	up(&N->err, std::vector<int>(1, 0));
 	if (e) {
 		fv_mpnn_destroy(N);
 		return cuda_status(e, "mpnn allocation");
@@ -951,6 +1394,13 @@ void fv_mpnn_destroy(fv_mpnn *N)
 	for (void *q : N->owned)
 		if (q) cudaFree(q);
 	delete N;
+}
+
+fv_status fv_mpnn_set_gemm_path(fv_mpnn *N, int path)
+{
+	if (!N || path < 0 || path > 1) { set_error("invalid argument"); return FV_ERR_INVALID; }
+	N->gemm_path = path;
+	return FV_OK;
 }
 
 fv_status fv_mpnn_set_scale(fv_mpnn *N, const float *scale4)
@@ -999,7 +1449,7 @@ fv_status fv_mpnn_predict(fv_mpnn *N, const fv_physics_cfg *phys, int batch, dou
 		e = cudaGetLastError();
 	}
 	if (!e) e = cudaStreamSynchronize(s);
-	return cuda_status(e, "mpnn predict");
+	return finish(N, e, "mpnn predict");
 }
 
 /* gradients of the mean squared error of y against the target state (host
@@ -1017,7 +1467,7 @@ fv_status fv_mpnn_gradients(fv_mpnn *N, const fv_physics_cfg *phys, int batch, c
 	if (!e) e = backward(N, batch, s);
 	if (!e && h_grad) e = cudaMemcpy(h_grad, N->g, sizeof(float) * N->lay.total, cudaMemcpyDeviceToHost);
 	if (!e) e = cudaStreamSynchronize(s);
-	return cuda_status(e, "mpnn gradients");
+	return finish(N, e, "mpnn gradients");
 }
 
 /* one Adam step on the mean squared error of y against the target states */

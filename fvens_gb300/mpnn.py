@@ -27,6 +27,7 @@ def _bind():
     L.fv_mpnn_destroy.argtypes = [vp]
     L.fv_mpnn_destroy.restype = None
     L.fv_mpnn_set_scale.argtypes = [vp, _F]
+    L.fv_mpnn_set_gemm_path.argtypes = [vp, ctypes.c_int]
     L.fv_mpnn_params.argtypes = [vp, _F, _F, ctypes.POINTER(ctypes.c_longlong)]
     L.fv_mpnn_graph.argtypes = [vp, _F, ctypes.POINTER(ctypes.c_int), _F]
     L.fv_mpnn_predict.argtypes = [vp, ctypes.POINTER(fv_physics_cfg), ctypes.c_int, vp]
@@ -61,6 +62,12 @@ class MPNN:
         """Per-variable scale of the output: u = uinf + scale * y."""
         self.scale = np.ascontiguousarray(scale, dtype=np.float32)
         check(_bind().fv_mpnn_set_scale(self._h, _fp(self.scale)))
+
+    def set_gemm_path(self, path):
+        """Tensor-core path of the forward cell GEMMs: "tcgen05"
+        (tensor-memory accumulators) or "mma_sync" (warp-level; the default,
+        faster for these row-bound GEMMs)."""
+        check(_bind().fv_mpnn_set_gemm_path(self._h, {"tcgen05": 0, "mma_sync": 1}[path]))
 
     def params(self, new=None):
         """The flat FP32 parameter vector (after loading `new` when given)."""
@@ -165,13 +172,24 @@ def train(net, phys, states, epochs, batch, lr, seed=0, lr_final=None, log=None)
     return losses
 
 
-def fallback_solve(main, start_solver, main_solver, u, stats):
-    """The fallback of a warm-started batch: members whose solve did not
-    converge (stats[k]["status"] != 0) restart from freestream with the starter
-    and the main solve (the method without the network); the others keep
-    their states.  Updates stats in place; returns the members that fell back."""
+def diverged(st):
+    """A judge for fallback_solve: the solve from the prediction failed
+    numerically (non-finite residual) or ended no lower than it started.  A
+    member that made progress but stalled or reached the step limit keeps its
+    result: a stall is a property of the condition (an unsteady or slowly
+    converging flow), which a freestream start meets as well."""
+    return st["status"] == 3 or (st["status"] != 0 and not st["res"] < st["res0"])
+
+
+def fallback_solve(main, start_solver, main_solver, u, stats, judge=None):
+    """The fallback of a warm-started batch: members whose solve from the
+    prediction is rejected -- judge(stats[k]) true; by default every member
+    that did not converge -- restart from freestream with the starter and the
+    main solve (the method without the network); the others keep their
+    states.  Updates stats in place; returns the members that fell back."""
     import torch
-    failed = [k for k, st in enumerate(stats) if st["status"] != 0]
+    judge = judge or (lambda st: st["status"] != 0)
+    failed = [k for k, st in enumerate(stats) if judge(st)]
     if failed:
         mask = np.zeros(len(stats), np.int32)
         mask[failed] = 1
@@ -186,12 +204,13 @@ def fallback_solve(main, start_solver, main_solver, u, stats):
     return failed
 
 
-def warm_started_solve(net, phys, main, start_solver, main_solver, u):
+def warm_started_solve(net, phys, main, start_solver, main_solver, u, judge=None):
     """Solves the conditions `phys` from the network's prediction and judges
-    the result: the main solve runs from the prediction, and members that do
-    not converge fall back to freestream with the starter (fallback_solve).
-    u: device array of the batch (filled here).  Returns (stats per member,
-    members that fell back)."""
+    the result: the main solve runs from the prediction, and members whose
+    solve is rejected (judge; by default every member that did not converge)
+    fall back to freestream with the starter (fallback_solve).  u: device
+    array of the batch (filled here).  Returns (stats per member, members that
+    fell back)."""
     net.predict(phys, u)
     _, stats = main_solver.solve(u, raise_on_error=False)
-    return stats, fallback_solve(main, start_solver, main_solver, u, stats)
+    return stats, fallback_solve(main, start_solver, main_solver, u, stats, judge)

@@ -384,6 +384,11 @@ fv_status fv_mpnn_create(fv_mesh *m, int layers, const int *wall_markers, int nw
                          fv_mpnn **out);
 void fv_mpnn_destroy(fv_mpnn *n);
 fv_status fv_mpnn_set_scale(fv_mpnn *n, const float *h_scale4);
+/* tensor-core path of the forward pass's cell GEMMs (node update, message
+ * MLP's first layer): 0 tcgen05.mma with tensor-memory accumulators, 1
+ * (default, the faster on GB300 for these row-bound GEMMs) warp-level
+ * mma.sync; both take BF16 operands and accumulate in FP32 */
+fv_status fv_mpnn_set_gemm_path(fv_mpnn *n, int path);
 /* copies the flat FP32 parameter vector in (h_in != NULL) and then out
  * (h_out != NULL); *count receives its length */
 fv_status fv_mpnn_params(fv_mpnn *n, float *h_out, const float *h_in, long long *count);

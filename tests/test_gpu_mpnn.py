@@ -25,10 +25,12 @@ def _random_params(net, seed, amp=0.15):
     return net.params(p)
 
 
-def test_forward_and_gradients_match_oracle(cuda):
+@pytest.mark.parametrize("path", ["tcgen05", "mma_sync"])
+def test_forward_and_gradients_match_oracle(cuda, path):
     import torch
     m = cases.channel(24, 8)
     net = MPNN(m, layers=2, wall_markers=(1, 3), seed=5)
+    net.set_gemm_path(path)
     p = _random_params(net, 7)
     scale = np.array([0.05, 0.1, 0.08, 0.3], np.float32)
     net.set_scale(scale)
@@ -54,6 +56,33 @@ def test_forward_and_gradients_match_oracle(cuda):
         n = int(np.prod(s))
         a, b = g[o:o + n], gref[o:o + n]
         assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b) + 1e-7, name
+
+
+def test_gemm_paths_agree_over_many_tiles(cuda):
+    """tcgen05 and mma.sync forward GEMMs on a batch large enough that every
+    CTA of the persistent GEMMs runs several tiles through its ring of staged
+    tiles (about 110k cell rows): the same outputs and gradients up to the
+    FP32 summation order."""
+    import torch
+    m = cases.channel(192, 64)
+    net = MPNN(m, layers=2, wall_markers=(1, 3), seed=4)
+    _random_params(net, 9)
+    net.set_scale(np.array([0.05, 0.1, 0.08, 0.3], np.float32))
+    phys, dicts = _conds([0.35, 0.42, 0.5, 0.57, 0.63, 0.7], [-2.0, -1.0, 0.0, 1.0, 2.0, 3.0])
+    _, uinf = M.conditions(dicts)
+    assert len(phys) * m.nelem > 100000
+    tgt = torch.tensor(uinf[:, None, :] + 0.02 * np.random.default_rng(1).normal(size=(len(phys), m.nelem, 4)),
+                       device=cuda)
+    out = {}
+    for path in ("tcgen05", "mma_sync"):
+        net.set_gemm_path(path)
+        u = torch.zeros((len(phys), m.nelem, 4), dtype=torch.float64, device=cuda)
+        net.predict(phys, u)
+        out[path] = (u.cpu().numpy() - uinf[:, None, :],) + net.gradients(phys, tgt)
+    (ya, la, ga), (yb, lb, gb) = out["tcgen05"], out["mma_sync"]
+    assert np.linalg.norm(ya - yb) <= 1e-5 * np.linalg.norm(yb)
+    assert abs(la - lb) <= 1e-5 * lb
+    assert np.linalg.norm(ga - gb) <= 1e-4 * np.linalg.norm(gb)
 
 
 def test_gradients_batch_additive(cuda):

@@ -63,3 +63,16 @@ def test_message_directions_and_aggregation():
     net = M.Net(xs, np.array([[0, 1]]), np.array([[1.0, 0.0, 0.0]]), 1, bf16_operands=False)
     assert list(net.src) == [0, 1] and list(net.dst) == [1, 0]
     assert np.allclose(net.ea, [[1, 0, 0], [-1, 0, 0]])
+
+
+def test_fallback_judge():
+    """The warm start's fallback restarts a member from freestream when its
+    solve from the prediction diverged or ended no lower than it started; a
+    member that converged, or made progress and then stalled or reached the
+    step limit, keeps its result."""
+    from fvens_gb300.mpnn import diverged
+    assert diverged(dict(status=3, res=float("nan"), res0=1.0))
+    assert diverged(dict(status=4, res=2.0, res0=1.0))
+    assert diverged(dict(status=4, res=float("nan"), res0=1.0))
+    assert not diverged(dict(status=4, res=1e-6, res0=1.0))
+    assert not diverged(dict(status=0, res=1e-11, res0=1.0))
