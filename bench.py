@@ -82,11 +82,17 @@ NCU_COUNTS = {
 }
 KERNEL_SOURCES = ["fvens_gb300/csrc/fv_residual_body.cuh", "fvens_gb300/csrc/fv_device.cuh",
                   "fvens_gb300/csrc/fv_residual.cu", "fvens_gb300/csrc/fv_core.cuh"]
+# DRAM traffic of one FP32 ILU(0) apply on this workload (the 10 colour launches
+# of k_fwd_parts / k_bwd_parts; ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum
+# -k regex:'k_fwd_parts|k_bwd_parts' -s 10 -c 10 on `python bench.py --kernel ilu --reps 5`),
+# valid for the sweep sources whose digest is `sources`
+NCU_ILU = {"sources": "7c7278857d475d24", "dram_bytes": 86501888}
+ILU_SOURCES = ["fvens_gb300/csrc/fv_linalg.cu", "fvens_gb300/csrc/fv_linalg.cuh"]
 
 
-def kernel_sources_digest():
+def kernel_sources_digest(files=None):
     h = hashlib.sha256()
-    for f in KERNEL_SOURCES:
+    for f in files or KERNEL_SOURCES:
         with open(os.path.join(ROOT, f), "rb") as fh:
             h.update(fh.read())
     return h.hexdigest()[:16]
@@ -345,6 +351,8 @@ def roofline(dom, kern, nfaces, hbm_peak, peak_src, dfma_rate):
     valid = NCU_COUNTS["sources"] == kernel_sources_digest()
     cnt = NCU_COUNTS.get(dom) if valid else None
     traffic = cnt["dram_bytes"] if cnt else None
+    if dom == "ilu0_apply" and NCU_ILU["sources"] == kernel_sources_digest(ILU_SOURCES):
+        traffic = NCU_ILU["dram_bytes"]
     if dom == "ilu0_apply" or cnt is None:
         out = dict(bound="hbm", kernel=dom, traffic=traffic, **hbm)
         if dom != "ilu0_apply":
@@ -1068,6 +1076,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="skip every comparison variant")
     ap.add_argument("--no-graph", action="store_true",
                     help="profiling aid: issue every launch from the host instead of replaying a CUDA graph")
+    ap.add_argument("--main-steps", type=int, default=0,
+                    help="profiling aid: cap the main solve at this many steps (the solve then reports status 4)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--e2e-solves", type=int, default=5, help="solves timed end to end through host buffers")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
@@ -1092,6 +1102,8 @@ def main():
     if args.no_graph:
         STARTER["use_graph"] = 0
         MAIN["use_graph"] = 0
+    if args.main_steps > 0:
+        MAIN["max_timesteps"] = args.main_steps
     if args.kernel:
         run_kernel(args)
     elif args.impl == "reference":

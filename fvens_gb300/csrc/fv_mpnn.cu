@@ -447,29 +447,35 @@ __device__ __forceinline__ int local_tiles(int ntiles)
 
 /* thread 0: the copies of the CTA's local tile i into ring slot i mod NST */
 template <class X, class Z>
-__device__ __forceinline__ void issue_tile(const X &x, const Z *z, int rows, int i, float *stg, uint64_t *bar)
+__device__ __forceinline__ void issue_tile(const X &x, const Z *z, int rows, int i, float *stg, uint64_t *bar,
+                                           bool arm_only = false)
 {
 	const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * GR, nr = min(GR, rows - row0);
 	float *st = stg + (size_t)s * (X::FLOATS + (z ? Z::FLOATS : 0));
 	mbar_arrive_expect_tx(&bar[s], x.bytes(nr) + (z ? z->bytes(nr) : 0u));
+	if (arm_only) return;  // the wait-limit test: the bytes announced never come, no copy is in flight
 	x.copy(st, row0, nr, &bar[s]);
 	if (z) z->copy(st + X::FLOATS, row0, nr, &bar[s]);
 }
 
 /* after a wait ran out: thread 0 waits (bounded) for the copies still in
  * flight into the ring, from local tile i on, and records the error */
-__device__ __forceinline__ void abort_ring(int i, int nloc, uint64_t *bar, int *err)
+__device__ __forceinline__ void abort_ring(int i, int nloc, uint64_t *bar, int *err, long long limit)
 {
 	if (threadIdx.x != 0) return;
-	for (int j = i; j < nloc && j < i + NST; j++) mbar_wait_bounded(&bar[j % NST], (j / NST) & 1, 200000000LL);
+	for (int j = i; j < nloc && j < i + NST; j++) mbar_wait_bounded(&bar[j % NST], (j / NST) & 1, limit);
 	atomicExch(err, 1);
 }
 
-/* k_gemm with the row operand staged by bulk copies (the weights as in k_gemm) */
+/* k_gemm with the row operand staged by bulk copies (the weights as in k_gemm).
+ * wait_test (the wait-limit test only): the CTA's first tile is announced on
+ * its barrier but never copied, and waits give up after ~10 ms of SM clocks,
+ * so every CTA takes the error path with no copy in flight for that slot. */
 template <int K, int N, bool TRANS, class BL, class E>
 __global__ void __launch_bounds__(GT) k_gemm_bulk(int rows, BL bl, const float *w, int ldw, int nvalid, int kvalid,
-                                                   E ep, int *err)
+                                                   E ep, int *err, int wait_test)
 {
+	const long long limit = wait_test ? 20000000LL : 2000000000LL;
 	static_assert(BL::K == K, "operand width");
 	extern __shared__ __align__(128) unsigned char smem[];
 	float *stg = reinterpret_cast<float *>(smem);                                   // [NST][BL::FLOATS]
@@ -485,7 +491,7 @@ __global__ void __launch_bounds__(GT) k_gemm_bulk(int rows, BL bl, const float *
 	}
 	__syncthreads();
 	if (threadIdx.x == 0)
-		for (int i = 0; i < NST && i < nloc; i++) issue_tile<BL, BL>(bl, nullptr, rows, i, stg, bar);
+		for (int i = 0; i < NST && i < nloc; i++) issue_tile<BL, BL>(bl, nullptr, rows, i, stg, bar, wait_test && i == 0);
 	if (!TRANS) {
 		stage_w<K, N>(w, ldw, nvalid, kvalid, sB);
 	} else {
@@ -496,7 +502,7 @@ __global__ void __launch_bounds__(GT) k_gemm_bulk(int rows, BL bl, const float *
 	}
 	for (int i = 0; i < nloc; i++) {
 		const int s = i % NST, row0 = ((int)blockIdx.x + i * (int)gridDim.x) * GR, nr = min(GR, rows - row0);
-		if (!mbar_wait_bounded(&bar[s], (i / NST) & 1)) abort_ = 1;
+		if (!mbar_wait_bounded(&bar[s], (i / NST) & 1, limit)) abort_ = 1;
 		const float *st = stg + (size_t)s * BL::FLOATS;
 		for (int e = threadIdx.x; e < GR * (K / 4); e += GT) {
 			const int rr = e / (K / 4), q = e - rr * (K / 4);
@@ -505,7 +511,7 @@ __global__ void __launch_bounds__(GT) k_gemm_bulk(int rows, BL bl, const float *
 		}
 		fence_proxy_async_smem();  // this thread's reads of the slot before the copy that refills it
 		__syncthreads();           // sA (and at i = 0 sB) ready; the slot is free
-		if (abort_) { abort_ring(i, nloc, bar, err); return; }
+		if (abort_) { abort_ring(i, nloc, bar, err, limit / 10); return; }
 		if (threadIdx.x == 0 && i + NST < nloc) issue_tile<BL, BL>(bl, nullptr, rows, i + NST, stg, bar);
 		float2 old[N / 8][2];
 		tile_old<N>(ep, row0, rows, old);
@@ -563,7 +569,7 @@ __global__ void __launch_bounds__(GT) k_wgrad_bulk(int rows, XL xl, ZL zl, float
 		}
 		fence_proxy_async_smem();
 		__syncthreads();
-		if (abort_) { abort_ring(i, nloc, bar, err); return; }
+		if (abort_) { abort_ring(i, nloc, bar, err, 200000000LL); return; }
 		if (threadIdx.x == 0 && i + NST < nloc) issue_tile(xl, &zl, rows, i + NST, stg, bar);
 		if (warp * 16 < N) {
 			for (int k0 = 0; k0 < GR; k0 += 16) {
@@ -1035,6 +1041,7 @@ struct fv_mpnn {
 	float *part = nullptr, *bpart = nullptr, *rtmp = nullptr, *lpart = nullptr;
 	int *err = nullptr;  // set by a kernel whose bulk-copy or MMA wait ran out of time
 	int gemm_path = 1;   // forward cell GEMMs: 0 tcgen05, 1 mma.sync (faster here: see k_gemm_tc)
+	int wait_test = 0;   // the wait-limit test (k_gemm_bulk)
 	std::vector<void *> owned;
 };
 
@@ -1147,7 +1154,7 @@ void gemm_bulk(fv_mpnn *N, size_t rows, BL bl, const float *w, int ldw, int nval
 	const size_t sm = sizeof(float) * NST * BL::FLOATS + sizeof(__nv_bfloat16) * (GR + Nn) * (K + 8);
 	auto *kern = k_gemm_bulk<K, Nn, TRANS, BL, E>;
 	const unsigned grid = resident_grid(kern, sm, nb(rows, GR), 4 * 152);
-	kern<<<grid, GT, sm, s>>>((int)rows, bl, w, ldw, nvalid, kvalid, ep, N->err);
+	kern<<<grid, GT, sm, s>>>((int)rows, bl, w, ldw, nvalid, kvalid, ep, N->err, N->wait_test);
 }
 
 /* forward pass for B members; activations kept for the backward pass */
@@ -1400,6 +1407,13 @@ fv_status fv_mpnn_set_gemm_path(fv_mpnn *N, int path)
 {
 	if (!N || path < 0 || path > 1) { set_error("invalid argument"); return FV_ERR_INVALID; }
 	N->gemm_path = path;
+	return FV_OK;
+}
+
+fv_status fv_mpnn_test_wait_limit(fv_mpnn *N, int on)
+{
+	if (!N) { set_error("null argument"); return FV_ERR_INVALID; }
+	N->wait_test = on ? 1 : 0;
 	return FV_OK;
 }
 

@@ -28,6 +28,7 @@ def _bind():
     L.fv_mpnn_destroy.restype = None
     L.fv_mpnn_set_scale.argtypes = [vp, _F]
     L.fv_mpnn_set_gemm_path.argtypes = [vp, ctypes.c_int]
+    L.fv_mpnn_test_wait_limit.argtypes = [vp, ctypes.c_int]
     L.fv_mpnn_params.argtypes = [vp, _F, _F, ctypes.POINTER(ctypes.c_longlong)]
     L.fv_mpnn_graph.argtypes = [vp, _F, ctypes.POINTER(ctypes.c_int), _F]
     L.fv_mpnn_predict.argtypes = [vp, ctypes.POINTER(fv_physics_cfg), ctypes.c_int, vp]

@@ -389,6 +389,10 @@ fv_status fv_mpnn_set_scale(fv_mpnn *n, const float *h_scale4);
  * (default, the faster on GB300 for these row-bound GEMMs) warp-level
  * mma.sync; both take BF16 operands and accumulate in FP32 */
 fv_status fv_mpnn_set_gemm_path(fv_mpnn *n, int path);
+/* test of the bounded waits (on != 0): the bulk-copy GEMMs announce their first
+ * tile on its mbarrier without copying it, so every wait for it runs out
+ * (after ~10 ms) and calls return FV_ERR_CUDA with the context still usable */
+fv_status fv_mpnn_test_wait_limit(fv_mpnn *n, int on);
 /* copies the flat FP32 parameter vector in (h_in != NULL) and then out
  * (h_out != NULL); *count receives its length */
 fv_status fv_mpnn_params(fv_mpnn *n, float *h_out, const float *h_in, long long *count);

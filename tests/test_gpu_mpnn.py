@@ -85,6 +85,29 @@ def test_gemm_paths_agree_over_many_tiles(cuda):
     assert np.linalg.norm(ga - gb) <= 1e-4 * np.linalg.norm(gb)
 
 
+def test_bounded_waits_report_an_error_and_leave_the_context_usable(cuda):
+    """The bulk-copy GEMMs' mbarrier waits are bounded: with the test switch
+    the first tile of every CTA is announced and never copied, every wait for
+    it runs out, the call reports FV_ERR_CUDA, and the next call on the same
+    network and context gives the same prediction as before."""
+    import torch
+    from fvens_gb300.mpnn import _bind
+    m = cases.channel(24, 8)
+    net = MPNN(m, layers=2, wall_markers=(1, 3), seed=5)
+    _random_params(net, 7)
+    net.set_scale(np.array([0.05, 0.1, 0.08, 0.3], np.float32))
+    phys, _ = _conds([0.45, 0.55], [1.0, -2.0])
+    u = [torch.zeros((2, m.nelem, 4), dtype=torch.float64, device=cuda) for _ in range(3)]
+    net.predict(phys, u[0])
+    fv.check(_bind().fv_mpnn_test_wait_limit(net._h, 1))
+    with pytest.raises(fv.FvensError) as e:
+        net.predict(phys, u[1])
+    assert e.value.status == fv.FV_ERR_CUDA and "ran out of time" in str(e.value)
+    fv.check(_bind().fv_mpnn_test_wait_limit(net._h, 0))
+    net.predict(phys, u[2])
+    assert torch.equal(u[2], u[0])
+
+
 def test_gradients_batch_additive(cuda):
     """The gradient of a batch is the count-weighted sum of the members'."""
     import torch

@@ -167,3 +167,38 @@ def test_flat_plate_skin_friction_matches_oracle_and_converges(cuda):
         cdsf.append(f[2])
     order = rc.flat_plate_order(meshes_, cdsf, exact)
     assert c["band"][0] <= order <= c["band"][1], (order, cdsf)
+
+
+def test_laminar_workload_member_matches_oracle_converged_solve(cuda):
+    """Converged-field parity on the batched laminar workload's mesh (the
+    reference's hybrid NACA 0012 mesh refined twice, 210,496 cells): member 0
+    of the seed-7 batch (M 0.550, AoA -0.48 deg, Re 3435) solved on the GPU's
+    FP32-preconditioned path to an absolute 1e-12 against the oracle's own
+    complete FP64 solve of the same condition to 1e-12 (committed fixture):
+    Cl, CDp and CDsf within 1e-8 relative, the state at the fixture's cells
+    (every cell touching the wall and 4,096 seeded ones) within 1e-7 of its
+    largest value."""
+    import os
+
+    import torch
+
+    import bench
+    path = bench.LAMINAR_FIXTURE.format(2)
+    z = np.load(path)
+    if "tolerance" not in z.files or float(z["tolerance"]) != 1e-12:
+        pytest.skip("the laminar fixture is not the 1e-12 solve")
+    assert int(z["members"][0]) == 0 and os.path.exists(path)
+    m, _ = bench._laminar_mesh(fv, 2)
+    ph = bench._laminar_conditions(fv, 64, 7)[:1]
+    main = fv.FlowFV(m, ph, fv.numerics_cfg(flux="ROE", gradient="LEASTSQUARES"), bench.LAMINAR_BCS)
+    start = fv.FlowFV(m, ph, fv.numerics_cfg(flux="ROE", gradient="NONE"), bench.LAMINAR_BCS)
+    cfg = dict(bench.LAMINAR_MAIN, tolerance=1e-12, max_timesteps=3000, stall_steps=0)
+    S1 = fv.SteadyBackwardEulerSolver(start, pc="ilu0", precision=4, **bench.LAMINAR_START)
+    S2 = fv.SteadyBackwardEulerSolver(main, pc="ilu0", precision=4, **cfg)
+    u = bench._freestream_field(torch, cuda, main, m.nelem)
+    S1.solve(u)
+    _, st = S2.solve(u)
+    assert st[0]["status"] == 0 and st[0]["res"] < 1e-12
+    (cmp,) = bench._vs_laminar_fixture(m, 2, main, u, [0])
+    assert max(cmp["cl_cdp_cdsf_rel_diff"]) <= 1e-8, cmp
+    assert cmp["state_rel_diff"] <= 1e-7, cmp
