@@ -483,7 +483,7 @@ def _freestream_field(torch, dev, disc, nelem):
 def _vs_laminar_fixture(m, levels, main, u, members):
     """Converged states and Cl / CDp / CDsf of the given batch members against
     the oracle's own converged solves of the same conditions (committed
-    fixture; None when absent)."""
+    fixture, solved to `oracle_tolerance`; None when absent)."""
     path = LAMINAR_FIXTURE.format(levels)
     if not os.path.exists(path):
         return None
@@ -499,7 +499,8 @@ def _vs_laminar_fixture(m, levels, main, u, members):
             continue
         ug = uv[k][inv[z["cells"]]]
         uo = z["states"][j]
-        out.append({"member": int(k), "state_rel_diff": float(np.abs(ug - uo).max() / np.abs(uo).max()),
+        out.append({"member": int(k), "oracle_tolerance": float(z["tolerance"]) if "tolerance" in z.files else 1e-10,
+                    "state_rel_diff": float(np.abs(ug - uo).max() / np.abs(uo).max()),
                     "cl_cdp_cdsf_rel_diff": [float(abs(fun[k, i] - z["functionals"][j, i]) /
                                                    max(abs(z["functionals"][j, i]), 1e-300)) for i in range(3)]})
     return out
@@ -1005,14 +1006,20 @@ def run_kernel(args):
             call = lambda: start.assemble_jacobian(u, A)
             what = f"FP32 first-order Jacobian ({m.nelem} cells)"
         else:
-            start.assemble_jacobian(u, A)
-            A.add_diagonal(torch.tensor(m.geometry()["area"] / 0.01, device=dev))  # pseudo-time term
-            P = fv.Preconditioner(start, A, "ilu0", part_size=args.part)
+            B = args.ilu_batch
+            disc = start
+            if B > 1:  # B copies of the workload's condition in one batched discretisation
+                disc = fv.FlowFV(m, [fv.physics_cfg(**PHYS)] * B, fv.numerics_cfg(**NUM_START), BCS)
+                u = u.repeat(B, 1)
+                A = fv.BlockMatrix(disc, 4)
+            disc.assemble_jacobian(u, A)
+            A.add_diagonal(torch.tensor(np.tile(m.geometry()["area"] / 0.01, B), device=dev))  # pseudo-time term
+            P = fv.Preconditioner(disc, A, "ilu0", part_size=args.part)
             P.setup()
-            x = torch.tensor(rng.normal(size=(m.nelem, 4)), device=dev)
+            x = torch.tensor(rng.normal(size=(B * m.nelem, 4)), device=dev)
             z = torch.zeros_like(x)
             call = lambda: P.apply(x, z)
-            what = f"FP32 ILU(0) apply ({m.nelem} cells, parts of <= {args.part})"
+            what = f"FP32 ILU(0) apply ({B} x {m.nelem} cells, parts of <= {args.part})"
     for _ in range(3):
         call()
     torch.cuda.synchronize()
@@ -1067,6 +1074,7 @@ def main():
     ap.add_argument("--reps", type=int, default=5, help="launches timed by --kernel")
     ap.add_argument("--part", type=int, default=128, help="--kernel ilu: cells per part of the block-colour order")
     ap.add_argument("--batch-members", type=int, default=16, help="--kernel mpnn: conditions per training step")
+    ap.add_argument("--ilu-batch", type=int, default=1, help="--kernel ilu: batch members (copies of the condition)")
     ap.add_argument("--small", action="store_true",
                     help="a 64 x 32 O-grid of the workload's family (CPU tests of the launch path; named so in "
                          "config.workload)")

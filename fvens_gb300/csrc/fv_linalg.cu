@@ -304,9 +304,26 @@ __global__ void __launch_bounds__(BS) k_bwd(int nelem, int p0, int p1, int sgs, 
  * one barrier per level. */
 constexpr int PT = 128;  // threads per part CTA (32 cells x 4 block rows per pass of a level)
 
-/* dynamic shared memory of the sweep kernels for parts of at most cap cells */
+/* dynamic shared memory of the sweep kernels for parts of at most cap cells
+ * with at most bcap in-part neighbour blocks on the sweep's side (lower for the
+ * forward, upper for the backward sweep), with or without inverted diagonals:
+ * only the blocks a part has are staged, so more parts fit on an SM */
 template <class R>
-size_t sweep_smem(int cap) { return (size_t)cap * (64 + 16 + 4 + 4) * sizeof(R) + (size_t)cap * sizeof(int4); }
+size_t sweep_smem(int cap, int bcap, bool diag)
+{
+	return ((size_t)bcap * 16 + (diag ? (size_t)cap * 16 : 0) + (size_t)cap * 8) * sizeof(R) +
+	       (size_t)cap * sizeof(int4);
+}
+/* Staging layout of a sweep launch.  A launch whose CTAs all fit on the machine
+ * at four per SM (one condition: a colour's parts) stages each cell's blocks at
+ * fixed slots (4 c + j), which measured faster there (one condition's apply
+ * 0.130 ms against 0.152 ms compact); a larger launch (a batch) stages only the
+ * blocks a part has (slots from pblk), so more CTAs fit on an SM and hide each
+ * other's latency (64 conditions: 3.40 -> 2.35 ms). */
+bool sweep_compact(const Precond &P, int parts) { return (size_t)parts * P.batch > (size_t)4 * P.num_sms; }
+
+/* a staged in-part neighbour: local index and block slot in one int (-1: none) */
+__device__ __forceinline__ int pack_nb(int loc, int slot) { return loc | (slot << 16); }
 /* ... and of the factorisation */
 template <class R>
 size_t ilu_smem(int cap) { return (size_t)cap * (80 + 16) * sizeof(R); }
@@ -317,18 +334,20 @@ __device__ __forceinline__ R dot4(const R *a, const R *v) { return a[0] * v[0] +
 /* forward sweep of the parts of one colour: y_p = r_i - sum_{lower} L y (ILU)
  * or Dinv (r_i - sum_{lower} A y) (SGS) */
 template <class R>
-__global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+__global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap, int bcap, int compact,
+                                                  const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const double *__restrict__ r, const int *__restrict__ pos_cell,
-                                                  const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
-                                                  const R *__restrict__ Dinv, R *__restrict__ y, const int *active)
+                                                  const int4 *__restrict__ pnbrpos, const int2 *__restrict__ pblk,
+                                                  const R *__restrict__ F, const R *__restrict__ Dinv,
+                                                  R *__restrict__ y, const int *active)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
-	R *sF = reinterpret_cast<R *>(smem);  // [cap][4][16] in-part lower blocks
-	R *sD = sF + (size_t)cap * 64;         // [cap][16]    Dinv (SGS)
-	R *sv = sD + (size_t)cap * 16;         // [cap][4]     y of the part
-	R *st = sv + (size_t)cap * 4;          // [cap][4]     right-hand side
-	int4 *snb = reinterpret_cast<int4 *>(st + (size_t)cap * 4);  // in-part lower neighbours (local), -1 none
+	R *sF = reinterpret_cast<R *>(smem);            // [bcap][16]  in-part lower blocks (bcap = 4 cap unless compact)
+	R *sD = sF + (size_t)bcap * 16;                  // [cap][16]   Dinv (SGS only)
+	R *sv = sD + (sgs ? (size_t)cap * 16 : 0);       // [cap][4]    y of the part
+	R *st = sv + (size_t)cap * 4;                    // [cap][4]    right-hand side
+	int4 *snb = reinterpret_cast<int4 *>(st + (size_t)cap * 4);  // in-part lower neighbours (pack_nb), -1 none
 	const int b = blockIdx.y;
 	if (member_off(active, b)) return;
 	const int part = part0 + blockIdx.x;
@@ -343,7 +362,7 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 		R s[4] = {R(rv.x), R(rv.y), R(rv.z), R(rv.w)};
 		const int4 np4 = pnbrpos[p];
 		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
-		int loc[4];
+		int loc[4], slot = compact ? pblk[p].x : 4 * c;
 		for (int j = 0; j < 4; j++) {
 			loc[j] = -1;
 			const int q = nbp[j];
@@ -351,8 +370,9 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 			R blk[16];
 			load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
 			if (q >= p0) {
-				loc[j] = q - p0;
-				store_blk(sF + ((size_t)c * 4 + j) * 16, blk);
+				const int sl = compact ? slot++ : 4 * c + j;
+				loc[j] = pack_nb(q - p0, sl);
+				store_blk(sF + (size_t)sl * 16, blk);
 			} else {
 				const R yy[4] = {yb[4 * (size_t)q], yb[4 * (size_t)q + 1], yb[4 * (size_t)q + 2], yb[4 * (size_t)q + 3]};
 				R t[4];
@@ -383,7 +403,7 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 					const int4 nb = snb[c];
 					const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
 					for (int j = 0; j < 4; j++)
-						if (l4[j] >= 0) acc -= dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+						if (l4[j] >= 0) acc -= dot4(sF + (size_t)(l4[j] >> 16) * 16 + 4 * row, sv + 4 * (l4[j] & 0xFFFF));
 				}
 				if (sgs) {
 					if (on) st[4 * c + row] = acc;
@@ -401,16 +421,17 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 /* backward sweep of the parts of one colour (levels in reverse):
  * z_i = Dinv (y_p - sum_{upper} U z) (ILU) or y_p - Dinv sum_{upper} A z (SGS) */
 template <class R>
-__global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap, const int *__restrict__ part_ptr,
+__global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap, int bcap, int compact,
+                                                  const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
-                                                  const int4 *__restrict__ pnbrpos, const R *__restrict__ F,
-                                                  const R *__restrict__ Dinv, const R *__restrict__ y,
-                                                  double *__restrict__ z, const int *active)
+                                                  const int4 *__restrict__ pnbrpos, const int2 *__restrict__ pblk,
+                                                  const R *__restrict__ F, const R *__restrict__ Dinv,
+                                                  const R *__restrict__ y, double *__restrict__ z, const int *active)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
-	R *sF = reinterpret_cast<R *>(smem);  // [cap][4][16] in-part upper blocks
-	R *sD = sF + (size_t)cap * 64;         // [cap][16]    Dinv
+	R *sF = reinterpret_cast<R *>(smem);  // [bcap][16]   in-part upper blocks
+	R *sD = sF + (size_t)bcap * 16;        // [cap][16]    Dinv
 	R *sv = sD + (size_t)cap * 16;         // [cap][4]     z of the part
 	R *st = sv + (size_t)cap * 4;          // [cap][4]     right-hand side (ILU) / outside sum (SGS)
 	int4 *snb = reinterpret_cast<int4 *>(st + (size_t)cap * 4);
@@ -428,7 +449,7 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 		const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
 		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
 		R s[4] = {R(0), R(0), R(0), R(0)};
-		int loc[4];
+		int loc[4], slot = compact ? pblk[p].y : 4 * c;
 		for (int j = 0; j < 4; j++) {
 			loc[j] = -1;
 			const int q = nbp[j];
@@ -436,8 +457,9 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 			R blk[16];
 			load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
 			if (q < p1) {
-				loc[j] = q - p0;
-				store_blk(sF + ((size_t)c * 4 + j) * 16, blk);
+				const int sl = compact ? slot++ : 4 * c + j;
+				loc[j] = pack_nb(q - p0, sl);
+				store_blk(sF + (size_t)sl * 16, blk);
 			} else {
 				const double4 zz = reinterpret_cast<const double4 *>(zb)[nbc[j]];
 				const R zv[4] = {R(zz.x), R(zz.y), R(zz.z), R(zz.w)};
@@ -469,7 +491,7 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 					const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
 					R acc = R(0);
 					for (int j = 0; j < 4; j++)
-						if (l4[j] >= 0) acc += dot4(sF + ((size_t)c * 4 + j) * 16 + 4 * row, sv + 4 * l4[j]);
+						if (l4[j] >= 0) acc += dot4(sF + (size_t)(l4[j] >> 16) * 16 + 4 * row, sv + 4 * (l4[j] & 0xFFFF));
 					// ILU: t = (y - outside) - inside;  SGS: t = outside + inside
 					st[4 * c + row] = sgs ? st[4 * c + row] + acc : st[4 * c + row] - acc;
 				}
@@ -952,15 +974,19 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 		for (int c = 0; c < P.ncolors; c++) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			k_fwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap), s>>>(
-			    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell, P.pnbrpos, F, D, y, active);
+			const int cm = sweep_compact(P, q1 - q0), bcap = cm ? P.blk_cap_lo : 4 * P.part_cap;
+			k_fwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap, bcap, sgs), s>>>(
+			    N, q0, P.part_cap, bcap, cm, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell, P.pnbrpos, P.pblk,
+			    F, D, y, active);
 			(*nk)++;
 		}
 		for (int c = P.ncolors - 1; c >= 0; c--) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			k_bwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap), s>>>(
-			    N, q0, P.part_cap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell, P.pnbr, P.pnbrpos, F, D, y, z, active);
+			const int cm = sweep_compact(P, q1 - q0), bcap = cm ? P.blk_cap_up : 4 * P.part_cap;
+			k_bwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap, bcap, true), s>>>(
+			    N, q0, P.part_cap, bcap, cm, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell, P.pnbr, P.pnbrpos,
+			    P.pblk, F, D, y, z, active);
 			(*nk)++;
 		}
 	} else {
@@ -1026,6 +1052,26 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 		pn[p] = make_int4(a[0], a[1], a[2], a[3]);
 		pp[p] = make_int4(c[0], c[1], c[2], c[3]);
 	}
+	// block colours: each cell's first slot among its part's in-part lower and upper
+	// neighbour blocks (the sweeps stage exactly these), and the fullest part's counts
+	std::vector<int2> pb;
+	if (P.ordering == 1) {
+		pb.resize(N);
+		for (size_t k = 0; k + 1 < part_ptr.size(); k++) {
+			const int p0 = part_ptr[k], p1 = part_ptr[k + 1];
+			int lo = 0, upc = 0;
+			for (int p = p0; p < p1; p++) {
+				pb[p] = make_int2(lo, upc);
+				const int q4[4] = {pp[p].x, pp[p].y, pp[p].z, pp[p].w};
+				for (int j = 0; j < 4; j++) {
+					if (q4[j] >= p0 && q4[j] < p) lo++;
+					if (q4[j] > p && q4[j] < p1) upc++;
+				}
+			}
+			P.blk_cap_lo = std::max(P.blk_cap_lo, lo);
+			P.blk_cap_up = std::max(P.blk_cap_up, upc);
+		}
+	}
 	cudaError_t e = cudaSuccess;
 	auto up = [&](void **d, const void *src, size_t bytes) {
 		if (e) return;
@@ -1037,21 +1083,35 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 	up((void **)&P.pnbr, pn.data(), sizeof(int4) * N);
 	up((void **)&P.pnbrpos, pp.data(), sizeof(int4) * N);
 	if (P.ordering == 1) {
+		up((void **)&P.pblk, pb.data(), sizeof(int2) * N);
 		up((void **)&P.part_ptr, part_ptr.data(), sizeof(int) * part_ptr.size());
 		up((void **)&P.lev_ptr, lev_ptr.data(), sizeof(int) * lev_ptr.size());
 		up((void **)&P.lev_pos, lev_pos.data(), sizeof(int) * lev_pos.size());
 	}
+	if (!e) {
+		int dev = 0;
+		e = cudaGetDevice(&dev);
+		if (!e) e = cudaDeviceGetAttribute(&P.num_sms, cudaDevAttrMultiProcessorCount, dev);
+	}
 	if (!e && P.ordering == 1) {
 		// shared memory of the part kernels beyond the 48 KB default
-		const int cap = std::max(P.part_cap, 1);
+		// (the sweeps' limit is set for the largest parts any preconditioner may have, since the
+		// setting is per kernel, not per preconditioner; a launch's own size sets its occupancy)
+		const int cap = std::max(P.part_cap, 1), big = kMaxPartSize;
 		if (prec == 4) {
-			e = cudaFuncSetAttribute(k_fwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<float>(cap));
-			if (!e) e = cudaFuncSetAttribute(k_bwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<float>(cap));
+			e = cudaFuncSetAttribute(k_fwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         (int)sweep_smem<float>(big, 4 * big, true));
+			if (!e)
+				e = cudaFuncSetAttribute(k_bwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                         (int)sweep_smem<float>(big, 4 * big, true));
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<float>(cap));
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<float>(cap));
 		} else {
-			e = cudaFuncSetAttribute(k_fwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>(cap));
-			if (!e) e = cudaFuncSetAttribute(k_bwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double>(cap));
+			e = cudaFuncSetAttribute(k_fwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         (int)sweep_smem<double>(big, 4 * big, true));
+			if (!e)
+				e = cudaFuncSetAttribute(k_bwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                         (int)sweep_smem<double>(big, 4 * big, true));
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<double, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<double>(cap));
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<double>(cap));
 		}
@@ -1065,10 +1125,10 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 
 void precond_free(Precond &P)
 {
-	void *ps[] = {P.pos_cell, P.cell_pos, P.pnbr, P.pnbrpos, P.F, P.Dinv, P.y, P.part_ptr, P.lev_ptr, P.lev_pos};
+	void *ps[] = {P.pos_cell, P.cell_pos, P.pnbr, P.pnbrpos, P.pblk, P.F, P.Dinv, P.y, P.part_ptr, P.lev_ptr, P.lev_pos};
 	for (void *p : ps)
 		if (p) cudaFree(p);
-	P.pos_cell = nullptr; P.cell_pos = nullptr; P.pnbr = nullptr; P.pnbrpos = nullptr;
+	P.pos_cell = nullptr; P.cell_pos = nullptr; P.pnbr = nullptr; P.pnbrpos = nullptr; P.pblk = nullptr;
 	P.F = nullptr; P.Dinv = nullptr; P.y = nullptr;
 	P.part_ptr = nullptr; P.lev_ptr = nullptr; P.lev_pos = nullptr;
 }

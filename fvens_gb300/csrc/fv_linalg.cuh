@@ -35,6 +35,10 @@ struct Precond {
 	int *cell_pos = nullptr;    // [nelem] position of cell i
 	int4 *pnbr = nullptr;       // [nelem] neighbours (as cells) of the cell at position p, -1 none
 	int4 *pnbrpos = nullptr;    // [nelem] their positions, -1 none
+	int2 *pblk = nullptr;       // [nelem] block colours: first shared-memory slot of the cell's in-part
+	                            // lower (x) and upper (y) neighbour blocks within its part
+	int blk_cap_lo = 0, blk_cap_up = 0;  // in-part lower / upper blocks of the fullest part
+	int num_sms = 1;            // SMs of the device (the sweeps' staging layout depends on the waves)
 	void *F = nullptr;          // [batch][5][nelem][16] factor / copy in colour order
 	void *Dinv = nullptr;       // [batch][nelem][16] inverted (factored) diagonal, colour order
 	void *y = nullptr;          // [batch][nelem][4] intermediate sweep vector, colour order

@@ -124,3 +124,42 @@ def test_line_aware_parts_match_oracle(cuda, kind):
     P.apply(torch.tensor(r, device=cuda), z)
     zo = orc.precond_apply(rp, col, val, kind, r.ravel(), order=order).reshape(-1, 4)
     assert np.abs(z.cpu().numpy() - zo).max() <= 1e-11 * np.abs(zo).max()
+
+
+@pytest.mark.parametrize("kind", ["ilu0", "sgs"])
+def test_batched_apply_with_compact_staging(cuda, kind):
+    """A batch large enough that a colour's sweep launch holds more CTAs than
+    four per SM (32 members x ~58 parts of 64 cells), where the sweeps stage
+    only the in-part blocks each part has: every member's apply equals the
+    single condition's apply (fixed staging slots) bit for bit, and the
+    oracle's to the FP32 tolerance."""
+    import torch
+    m = cases.channel(192, 64)
+    B = 32
+    ph = fv.physics_cfg(Minf=0.5)
+    num = fv.numerics_cfg(flux="ROE")
+    g1 = fv.FlowFV(m, ph, num, cases.CHANNEL_BCS)
+    gB = fv.FlowFV(m, [ph] * B, num, cases.CHANNEL_BCS)
+    od = orc.Disc(orc.Mesh.from_export(m.export()), Minf=0.5, flux="ROE", bcs=cases.CHANNEL_BCS)
+    u = cases.perturbed_state(od.freestream(), m.nelem)
+    _, dt = od.residual(u)
+    diag = m.geometry()["area"] / (50.0 * dt)
+    A1, AB = fv.BlockMatrix(g1, 4), fv.BlockMatrix(gB, 4)
+    g1.assemble_jacobian(torch.tensor(u, device=cuda), A1)
+    gB.assemble_jacobian(torch.tensor(np.tile(u, (B, 1)), device=cuda), AB)
+    A1.add_diagonal(torch.tensor(diag, device=cuda))
+    AB.add_diagonal(torch.tensor(np.tile(diag, B), device=cuda))
+    P1 = fv.Preconditioner(g1, A1, kind, ordering=1, part_size=64)
+    PB = fv.Preconditioner(gB, AB, kind, ordering=1, part_size=64)
+    P1.setup()
+    PB.setup()
+    r = np.random.default_rng(11).normal(size=(m.nelem, 4))
+    z1 = torch.zeros((m.nelem, 4), dtype=torch.float64, device=cuda)
+    zB = torch.zeros((B * m.nelem, 4), dtype=torch.float64, device=cuda)
+    P1.apply(torch.tensor(r, device=cuda), z1)
+    PB.apply(torch.tensor(np.tile(r, (B, 1)), device=cuda), zB)
+    for k in range(B):
+        assert torch.equal(zB[k * m.nelem:(k + 1) * m.nelem], z1), k
+    rp, col, val = A1.to_host()
+    zo = orc.precond_apply(rp, col, val, kind, r.ravel(), order=P1.order()).reshape(-1, 4)
+    assert np.abs(z1.cpu().numpy() - zo).max() <= 3e-5 * np.abs(zo).max()

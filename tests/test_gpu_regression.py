@@ -196,7 +196,7 @@ def test_laminar_workload_member_matches_oracle_converged_solve(cuda):
     S1 = fv.SteadyBackwardEulerSolver(start, pc="ilu0", precision=4, **bench.LAMINAR_START)
     S2 = fv.SteadyBackwardEulerSolver(main, pc="ilu0", precision=4, **cfg)
     u = bench._freestream_field(torch, cuda, main, m.nelem)
-    S1.solve(u)
+    S1.solve(u, raise_on_error=False)  # the starter may stop at its 50-step limit
     _, st = S2.solve(u)
     assert st[0]["status"] == 0 and st[0]["res"] < 1e-12
     (cmp,) = bench._vs_laminar_fixture(m, 2, main, u, [0])
