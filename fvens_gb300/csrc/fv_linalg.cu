@@ -315,15 +315,27 @@ size_t sweep_smem(int cap, int bcap, bool diag)
 	       (size_t)cap * sizeof(int4);
 }
 /* Staging layout of a sweep launch.  A launch whose CTAs all fit on the machine
- * at four per SM (one condition: a colour's parts) stages each cell's blocks at
- * fixed slots (4 c + j), which measured faster there (one condition's apply
- * 0.130 ms against 0.152 ms compact); a larger launch (a batch) stages only the
- * blocks a part has (slots from pblk), so more CTAs fit on an SM and hide each
- * other's latency (64 conditions: 3.40 -> 2.35 ms). */
+ * at four per SM (one condition: a colour's parts) is bound by each part's
+ * dependency chain; it stages each cell's blocks at fixed slots (4 c + j), so a
+ * level reads a block at an address that does not wait for the neighbour entry
+ * (one condition's apply 0.126 ms; 0.152 ms with the slots of the compact
+ * layout).  A larger launch (a batch) stages only the blocks a part has (slots
+ * from pblk), so more CTAs fit on an SM and hide each other's latency (64
+ * conditions: 3.40 -> 2.37 ms). */
 bool sweep_compact(const Precond &P, int parts) { return (size_t)parts * P.batch > (size_t)4 * P.num_sms; }
 
-/* a staged in-part neighbour: local index and block slot in one int (-1: none) */
+/* a staged in-part neighbour: with compact staging its local index and block
+ * slot in one int, else its local index (slot 4 c + j) (-1: none) */
 __device__ __forceinline__ int pack_nb(int loc, int slot) { return loc | (slot << 16); }
+template <bool COMPACT>
+__device__ __forceinline__ int nb_loc(int v) { return COMPACT ? (v & 0xFFFF) : v; }
+/* the staged block of cell c's neighbour j (entry v); with fixed slots its
+ * address does not wait for the neighbour entry */
+template <class R, bool COMPACT>
+__device__ __forceinline__ const R *blk_at(const R *sF, int c, int j, int v)
+{
+	return COMPACT ? sF + (size_t)(v >> 16) * 16 : sF + ((size_t)c * 4 + j) * 16;
+}
 /* ... and of the factorisation */
 template <class R>
 size_t ilu_smem(int cap) { return (size_t)cap * (80 + 16) * sizeof(R); }
@@ -333,8 +345,8 @@ __device__ __forceinline__ R dot4(const R *a, const R *v) { return a[0] * v[0] +
 
 /* forward sweep of the parts of one colour: y_p = r_i - sum_{lower} L y (ILU)
  * or Dinv (r_i - sum_{lower} A y) (SGS) */
-template <class R>
-__global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap, int bcap, int compact,
+template <class R, bool COMPACT>
+__global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap, int bcap,
                                                   const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const double *__restrict__ r, const int *__restrict__ pos_cell,
@@ -362,7 +374,7 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 		R s[4] = {R(rv.x), R(rv.y), R(rv.z), R(rv.w)};
 		const int4 np4 = pnbrpos[p];
 		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
-		int loc[4], slot = compact ? pblk[p].x : 4 * c;
+		int loc[4], slot = COMPACT ? pblk[p].x : 0;
 		for (int j = 0; j < 4; j++) {
 			loc[j] = -1;
 			const int q = nbp[j];
@@ -370,9 +382,14 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 			R blk[16];
 			load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
 			if (q >= p0) {
-				const int sl = compact ? slot++ : 4 * c + j;
-				loc[j] = pack_nb(q - p0, sl);
-				store_blk(sF + (size_t)sl * 16, blk);
+				if (COMPACT) {
+					loc[j] = pack_nb(q - p0, slot);
+					store_blk(sF + (size_t)slot * 16, blk);
+					slot++;
+				} else {
+					loc[j] = q - p0;
+					store_blk(sF + ((size_t)c * 4 + j) * 16, blk);
+				}
 			} else {
 				const R yy[4] = {yb[4 * (size_t)q], yb[4 * (size_t)q + 1], yb[4 * (size_t)q + 2], yb[4 * (size_t)q + 3]};
 				R t[4];
@@ -403,7 +420,7 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 					const int4 nb = snb[c];
 					const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
 					for (int j = 0; j < 4; j++)
-						if (l4[j] >= 0) acc -= dot4(sF + (size_t)(l4[j] >> 16) * 16 + 4 * row, sv + 4 * (l4[j] & 0xFFFF));
+						if (l4[j] >= 0) acc -= dot4(blk_at<R, COMPACT>(sF, c, j, l4[j]) + 4 * row, sv + 4 * nb_loc<COMPACT>(l4[j]));
 				}
 				if (sgs) {
 					if (on) st[4 * c + row] = acc;
@@ -420,8 +437,8 @@ __global__ void __launch_bounds__(PT) k_fwd_parts(int nelem, int part0, int cap,
 
 /* backward sweep of the parts of one colour (levels in reverse):
  * z_i = Dinv (y_p - sum_{upper} U z) (ILU) or y_p - Dinv sum_{upper} A z (SGS) */
-template <class R>
-__global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap, int bcap, int compact,
+template <class R, bool COMPACT>
+__global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap, int bcap,
                                                   const int *__restrict__ part_ptr,
                                                   const int *__restrict__ lev_ptr, const int *__restrict__ lev_pos,
                                                   int sgs, const int *__restrict__ pos_cell, const int4 *__restrict__ pnbr,
@@ -449,7 +466,7 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 		const int nbc[4] = {nb4.x, nb4.y, nb4.z, nb4.w};
 		const int nbp[4] = {np4.x, np4.y, np4.z, np4.w};
 		R s[4] = {R(0), R(0), R(0), R(0)};
-		int loc[4], slot = compact ? pblk[p].y : 4 * c;
+		int loc[4], slot = COMPACT ? pblk[p].y : 0;
 		for (int j = 0; j < 4; j++) {
 			loc[j] = -1;
 			const int q = nbp[j];
@@ -457,9 +474,14 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 			R blk[16];
 			load_blk(Fb + ((size_t)(1 + j) * N + p) * 16, blk);
 			if (q < p1) {
-				const int sl = compact ? slot++ : 4 * c + j;
-				loc[j] = pack_nb(q - p0, sl);
-				store_blk(sF + (size_t)sl * 16, blk);
+				if (COMPACT) {
+					loc[j] = pack_nb(q - p0, slot);
+					store_blk(sF + (size_t)slot * 16, blk);
+					slot++;
+				} else {
+					loc[j] = q - p0;
+					store_blk(sF + ((size_t)c * 4 + j) * 16, blk);
+				}
 			} else {
 				const double4 zz = reinterpret_cast<const double4 *>(zb)[nbc[j]];
 				const R zv[4] = {R(zz.x), R(zz.y), R(zz.z), R(zz.w)};
@@ -491,7 +513,7 @@ __global__ void __launch_bounds__(PT) k_bwd_parts(int nelem, int part0, int cap,
 					const int l4[4] = {nb.x, nb.y, nb.z, nb.w};
 					R acc = R(0);
 					for (int j = 0; j < 4; j++)
-						if (l4[j] >= 0) acc += dot4(sF + (size_t)(l4[j] >> 16) * 16 + 4 * row, sv + 4 * (l4[j] & 0xFFFF));
+						if (l4[j] >= 0) acc += dot4(blk_at<R, COMPACT>(sF, c, j, l4[j]) + 4 * row, sv + 4 * nb_loc<COMPACT>(l4[j]));
 					// ILU: t = (y - outside) - inside;  SGS: t = outside + inside
 					st[4 * c + row] = sgs ? st[4 * c + row] + acc : st[4 * c + row] - acc;
 				}
@@ -974,18 +996,24 @@ cudaError_t precond_apply_t(const Precond &P, const double *r, double *z, const 
 		for (int c = 0; c < P.ncolors; c++) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			const int cm = sweep_compact(P, q1 - q0), bcap = cm ? P.blk_cap_lo : 4 * P.part_cap;
-			k_fwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap, bcap, sgs), s>>>(
-			    N, q0, P.part_cap, bcap, cm, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell, P.pnbrpos, P.pblk,
+			const bool cm = sweep_compact(P, q1 - q0);
+			const int bcap = cm ? P.blk_cap_lo : 4 * P.part_cap;
+			auto *kern = cm ? k_fwd_parts<R, true> : k_fwd_parts<R, false>;
+			// (fixed slots: the staging size of the inverted diagonals too, as one part per
+			// launch was measured with)
+			kern<<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap, bcap, cm ? (bool)sgs : true), s>>>(
+			    N, q0, P.part_cap, bcap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, r, P.pos_cell, P.pnbrpos, P.pblk,
 			    F, D, y, active);
 			(*nk)++;
 		}
 		for (int c = P.ncolors - 1; c >= 0; c--) {
 			const int q0 = P.cpart[c], q1 = P.cpart[c + 1];
 			if (q1 <= q0) continue;
-			const int cm = sweep_compact(P, q1 - q0), bcap = cm ? P.blk_cap_up : 4 * P.part_cap;
-			k_bwd_parts<R><<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap, bcap, true), s>>>(
-			    N, q0, P.part_cap, bcap, cm, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell, P.pnbr, P.pnbrpos,
+			const bool cm = sweep_compact(P, q1 - q0);
+			const int bcap = cm ? P.blk_cap_up : 4 * P.part_cap;
+			auto *kern = cm ? k_bwd_parts<R, true> : k_bwd_parts<R, false>;
+			kern<<<dim3(q1 - q0, B), PT, sweep_smem<R>(P.part_cap, bcap, true), s>>>(
+			    N, q0, P.part_cap, bcap, P.part_ptr, P.lev_ptr, P.lev_pos, sgs, P.pos_cell, P.pnbr, P.pnbrpos,
 			    P.pblk, F, D, y, z, active);
 			(*nk)++;
 		}
@@ -1099,19 +1127,17 @@ cudaError_t precond_alloc(Precond &P, fv_mesh_impl *m, int batch, int type, int 
 		// setting is per kernel, not per preconditioner; a launch's own size sets its occupancy)
 		const int cap = std::max(P.part_cap, 1), big = kMaxPartSize;
 		if (prec == 4) {
-			e = cudaFuncSetAttribute(k_fwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                         (int)sweep_smem<float>(big, 4 * big, true));
-			if (!e)
-				e = cudaFuncSetAttribute(k_bwd_parts<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-				                         (int)sweep_smem<float>(big, 4 * big, true));
+			const int lim = (int)sweep_smem<float>(big, 4 * big, true);
+			for (const void *k : {(const void *)k_fwd_parts<float, false>, (const void *)k_fwd_parts<float, true>,
+			                      (const void *)k_bwd_parts<float, false>, (const void *)k_bwd_parts<float, true>})
+				if (!e) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<float>(cap));
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<float>(cap));
 		} else {
-			e = cudaFuncSetAttribute(k_fwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                         (int)sweep_smem<double>(big, 4 * big, true));
-			if (!e)
-				e = cudaFuncSetAttribute(k_bwd_parts<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-				                         (int)sweep_smem<double>(big, 4 * big, true));
+			const int lim = (int)sweep_smem<double>(big, 4 * big, true);
+			for (const void *k : {(const void *)k_fwd_parts<double, false>, (const void *)k_fwd_parts<double, true>,
+			                      (const void *)k_bwd_parts<double, false>, (const void *)k_bwd_parts<double, true>})
+				if (!e) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<double, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<double>(cap));
 			if (!e) e = cudaFuncSetAttribute(k_ilu_parts<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ilu_smem<double>(cap));
 		}
