@@ -761,7 +761,7 @@ def run_large(fv, torch, dev, peak_gbs, solve=True):
 
 LARGE_STARTER = dict(cfl_min=25, cfl_max=500, tolerance=1e-1, abs_tolerance=0, max_timesteps=100, nl_update=2,
                      min_relax=0.2, pc="ilu0")
-LARGE_MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=300, nl_update=2,
+LARGE_MAIN = dict(cfl_min=100, cfl_max=5000, tolerance=1e-10, abs_tolerance=1, max_timesteps=100, nl_update=2,
                   min_relax=0.2, pc="ilu0", matrix_free=1)
 
 
@@ -1103,8 +1103,9 @@ def main():
     ap.add_argument("--no-large", dest="large", action="store_false", help="skip the ~4M-cell variant")
     ap.add_argument("--no-large-solve", dest="large_solve", action="store_false",
                     help="~4M-cell variant: kernel times only, no end-to-end solves")
-    ap.add_argument("--large-steps", type=int, default=300,
-                    help="~4M-cell variant: main-solve step limit of the end-to-end solves")
+    ap.add_argument("--large-steps", type=int, default=100,
+                    help="~4M-cell variant: main-solve step limit of the end-to-end solves (the Barth-Jespersen "
+                         "solve does not converge on this mesh; the two paths are compared per step)")
     args = ap.parse_args()
     LARGE_MAIN["max_timesteps"] = args.large_steps
     if args.no_graph:
