@@ -82,3 +82,26 @@ def test_refined_hybrid_mesh_builds():
     assert (m.nelem, m.nbface) == (16 * base.nelem, 4 * base.nbface)
     a, a0 = m.geometry()["area"], base.geometry()["area"]
     assert a.min() > 0 and abs(a.sum() - a0.sum()) <= 1e-12 * a0.sum()
+
+
+def test_laminar_fixture_samples_the_refined_mesh():
+    """The oracle's converged-solve fixture of the laminar workload: solved to
+    1e-12, its sampled cells are cells of the twice-refined mesh in the
+    refinement's numbering and include every cell touching the wall, and the
+    sampled states are physical (positive density and energy)."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    f = np.load(os.path.join(here, "golden", "naca0012_laminar_l2_oracle_converged.npz"))
+    z = np.load(os.path.join(here, "golden", "naca0012_lam_hybrid_1_mesh.npz"))
+    r = meshes.refine(dict(coords=z["coords"], nnode=z["nnode"], inpoel=z["inpoel"], bface=z["bface"],
+                           btag=z["btag"]), 2)
+    nelem = len(r["nnode"])
+    assert float(f["tolerance"]) == 1e-12 and list(f["members"]) == [0]
+    cells = f["cells"]
+    assert cells.min() >= 0 and cells.max() < nelem and len(np.unique(cells)) == len(cells)
+    wall_nodes = np.unique(r["bface"][r["btag"] == 2])
+    near_wall = np.where(np.isin(r["inpoel"], wall_nodes).any(axis=1))[0]
+    assert np.isin(near_wall, cells).all()
+    u = f["states"][0]
+    assert u.shape == (len(cells), 4) and (u[:, 0] > 0).all() and (u[:, 3] > 0).all()
+    steps = f["solve_counts"][0]
+    assert steps[2] > 0 and np.isfinite(f["functionals"]).all()
