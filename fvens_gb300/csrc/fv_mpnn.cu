@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(GT) k_gemm_bulk(int rows, BL bl, const float *
 {
 	const long long limit = wait_test ? 20000000LL : 2000000000LL;
 	static_assert(BL::K == K, "operand width");
-	extern __shared__ __align__(128) unsigned char smem[];
+	extern __shared__ __align__(16) unsigned char smem[];
 	float *stg = reinterpret_cast<float *>(smem);                                   // [NST][BL::FLOATS]
 	__nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(stg + NST * BL::FLOATS);  // [64][K + 8]
 	__nv_bfloat16 *sB = sA + GR * (K + 8);                                          // [N][K + 8]
@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(GT) k_wgrad_bulk(int rows, XL xl, ZL zl, float
 	static_assert(XL::K == K && ZL::K == N, "operand widths");
 	static_assert(GT % (N / 4) == 0, "a thread stages the same column quad of dZ in every row");
 	constexpr int SLOT = XL::FLOATS + ZL::FLOATS;
-	extern __shared__ __align__(128) unsigned char smem[];
+	extern __shared__ __align__(16) unsigned char smem[];
 	float *stg = reinterpret_cast<float *>(smem);                                // [NST][SLOT]
 	__nv_bfloat16 *sZ = reinterpret_cast<__nv_bfloat16 *>(stg + NST * SLOT);    // [64][N + 8]
 	__nv_bfloat16 *sX = sZ + GR * (N + 8);                                       // [64][K + 8]
@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(GT) k_gemm_tc(int rows, PL pl, const float *w,
 	static_assert(PL::K == K && K % 16 == 0 && N % 16 == 0 && N >= 32 && N <= 256 && GT == TM, "tile shape");
 	constexpr unsigned LBO_A = TM * 16, LBO_B = N * 16;  // bytes between K-chunks (8-row groups adjacent)
 	constexpr uint32_t IDESC = tc_idesc_bf16(TM, N);
-	extern __shared__ __align__(128) unsigned char smem[];
+	extern __shared__ __align__(16) unsigned char smem[];
 	unsigned char *sA = smem;                                           // [K / 8][TM][16 B]
 	unsigned char *sB = sA + (size_t)TM * K * 2;                        // [K / 8][N][16 B]
 	float *stg = reinterpret_cast<float *>(sB + (size_t)N * K * 2);     // [NST][PL::FLOATS]
