@@ -14,12 +14,16 @@ with the natural order the oracle's solve of member 0 stalls at 1.4e-6 after
 
     python tests/golden/make_laminar_converged.py [levels] [members] [threads] [tol]
 
+The committed fixture holds members 0, 1 and 4 (`2 0,1,4 8 1e-12`; made as
+member 0 and members 1,4 in two runs and concatenated, the same arrays).
+
 Stored per member: the converged state at 4,096 seeded cells and at every
 cell touching the wall (`cells`, `states`), Cl / CDp / CDsf (`functionals`)
 and the step and Krylov counts.  bench.py compares the GPU's converged batch
-members with it, and tests/test_gpu_regression.py a GPU solve of member 0 to
-the same tolerance.  At 1e-10, member 0 took 2,443 s on 7 x86 threads (50 +
-681 steps, 1,128 + 18,664 Krylov iterations).
+members with it, and tests/test_gpu_regression.py a GPU batch of the same
+members solved to the same tolerance.  On 8 x86 threads at 1e-12: member 0
+3,509 s (50 + 1,043 steps), member 1 2,588 s (50 + 1,199), member 4 4,129 s
+(50 + 1,613); member 0 at 1e-10: 2,443 s on 7 threads (50 + 681 steps).
 """
 import os
 import sys
